@@ -1,0 +1,288 @@
+"""ctypes front end of the CPU oracle (oracle.cpp) and of the host build of the
+reference's own kernels (ref_host_driver.cpp + make_ref.py).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, always as the checker, never as the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+
+STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
+                "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
+
+SHIPPED, FIXED = 0, 1
+
+
+def build(force: bool = False) -> Path:
+    """Compile oracle.cpp (g++, OpenMP, no FP contraction so results match on x86 and Arm)."""
+    src = HERE / "oracle.cpp"
+    if LIB.exists() and not force and LIB.stat().st_mtime >= src.stat().st_mtime:
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    tmp = BUILD / f"liboracle.{os.getpid()}.so"
+    subprocess.run(["g++", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17",
+                    str(src), "-o", str(tmp)], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(str(build()))
+        vp, i, ll, d = C.c_void_p, C.c_int, C.c_longlong, C.c_double
+        L.orc_grid_dim.argtypes = [i]
+        L.orc_grid_dim.restype = i
+        L.orc_cell_of.argtypes = [C.c_float, C.c_float, C.c_float, i]
+        L.orc_cell_of.restype = i
+        L.orc_grid_sort.argtypes = [vp, i, i, vp, vp]
+        L.orc_knn.argtypes = [vp, i, vp, vp, i, i, i, vp, vp, i]
+        L.orc_tet_centroids.argtypes = [vp, vp, i, vp]
+        L.orc_tet_k.argtypes = [i, i, i]
+        L.orc_tet_k.restype = i
+        L.orc_tet_cell.argtypes = [i, vp, i, vp, i, vp, vp, i, vp, i, vp, vp, vp, vp, vp, i]
+        L.orc_cell_tet.argtypes = [i, vp, i, vp, i, vp, vp, i, vp, i, vp, vp, vp, i]
+        L.orc_lloyd_update.argtypes = [i, vp, i, vp, vp]
+        L.orc_mesh_volume.argtypes = [vp, vp, i]
+        L.orc_mesh_volume.restype = d
+        _lib = L
+    return _lib
+
+
+def grid_dim(n: int) -> int:
+    return lib().orc_grid_dim(n)
+
+
+def grid_sort(pts, dim: int):
+    """Stable counting sort by grid cell: (order sorted->original, cell_start)."""
+    pts = _f32(pts)
+    n = len(pts)
+    order = np.empty(n, np.int32)
+    cs = np.empty(dim ** 3 + 1, np.int32)
+    lib().orc_grid_sort(_p(pts), n, dim, _p(order), _p(cs))
+    return order, cs
+
+
+def knn(ref, qry=None, k: int = 64, key=None, exclude_self: bool | None = None, nthreads: int = 0):
+    """Exact kNN by (distance, key).  qry=None means the reference points query
+    themselves with self excluded.  Returns (indices into ref, squared distances)."""
+    ref = _f32(ref)
+    if qry is None:
+        qry = ref
+        if exclude_self is None:
+            exclude_self = True
+    qry = _f32(qry)
+    key = _i32(key) if key is not None else None
+    nq = len(qry)
+    idx = np.empty((nq, k), np.int32)
+    dd = np.empty((nq, k), np.float32)
+    lib().orc_knn(_p(ref), len(ref), _p(key), _p(qry), nq, k, int(bool(exclude_self)), _p(idx), _p(dd), nthreads)
+    return idx, dd
+
+
+def tet_centroids(verts, tets):
+    verts, tets = _f32(verts), _i32(tets)
+    out = np.empty((len(tets), 3), np.float32)
+    lib().orc_tet_centroids(_p(verts), _p(tets), len(tets), _p(out))
+    return out
+
+
+def tet_k(n_site: int, n_tet: int, preferred: int = 0) -> int:
+    return lib().orc_tet_k(n_site, n_tet, preferred)
+
+
+def tet_cell(sites, nbr, verts, tets, cand, mode: int = FIXED, pair_status: bool = False, nthreads: int = 0):
+    """Tet-cell method over all candidate pairs.  Returns dict with vol (n,),
+    mom (n,3) first moments, hist (14,) [0:7] non-contributing / [7:14]
+    contributing pair statuses, counters (5,), and optionally per-pair codes."""
+    sites, nbr, verts, tets, cand = _f32(sites), _i32(nbr), _f32(verts), _i32(tets), _i32(cand)
+    n, K = nbr.shape
+    nt, tk = cand.shape
+    vol = np.zeros(n, np.float64)
+    mom = np.zeros((n, 3), np.float64)
+    hist = np.zeros(14, np.int64)
+    ctr = np.zeros(5, np.int64)
+    ps = np.empty((nt, tk), np.int32) if pair_status else None
+    lib().orc_tet_cell(mode, _p(sites), n, _p(nbr), K, _p(verts), _p(tets), nt, _p(cand), tk,
+                       _p(vol), _p(mom), _p(hist), _p(ps), _p(ctr), nthreads)
+    out = dict(vol=vol, mom=mom, hist=hist, counters=ctr)
+    if pair_status:
+        out["pair_status"] = ps
+    return out
+
+
+def cell_tet(sites, nbr, verts, tets, cand, mode: int = FIXED, nthreads: int = 0):
+    sites, nbr, verts, tets, cand = _f32(sites), _i32(nbr), _f32(verts), _i32(tets), _i32(cand)
+    n, K = nbr.shape
+    nt, tk = cand.shape
+    vol = np.zeros(n, np.float64)
+    mom = np.zeros((n, 3), np.float64)
+    hist = np.zeros(14, np.int64)
+    lib().orc_cell_tet(mode, _p(sites), n, _p(nbr), K, _p(verts), _p(tets), nt, _p(cand), tk,
+                       _p(vol), _p(mom), _p(hist), nthreads)
+    return dict(vol=vol, mom=mom, hist=hist)
+
+
+def lloyd_update(sites, vol, mom, mode: int = FIXED):
+    s = _f32(sites).copy()
+    lib().orc_lloyd_update(mode, _p(s), len(s), _p(np.ascontiguousarray(vol, np.float64)),
+                           _p(np.ascontiguousarray(mom, np.float64)))
+    return s
+
+
+def mesh_volume(verts, tets) -> float:
+    verts, tets = _f32(verts), _i32(tets)
+    return lib().orc_mesh_volume(_p(verts), _p(tets), len(tets))
+
+
+def iteration(sites, verts, tets, K: int, tk: int = 0, ids=None, mode: int = FIXED, nthreads: int = 0):
+    """One Lloyd iteration of the path, restated end to end.
+
+    sites: (n,3) float32 in [0,1000]^3, ids: original id of each site (default
+    0..n-1).  Steps: grid sort by (cell, id); K nearest neighbours of every
+    site by (distance, id), self excluded; tet centroids; the tk nearest sites
+    of every centroid by (distance, id); tet-cell clipping; moments; update.
+    Everything after the sort is in sorted order.  Returns a dict.
+    """
+    sites = _f32(sites)
+    n = len(sites)
+    ids = np.arange(n, dtype=np.int32) if ids is None else _i32(ids)
+    dim = grid_dim(n)
+    # sort key (cell, id): counting sort of the id-ordered points is stable in id
+    by_id = np.argsort(ids, kind="stable")
+    order_local, cs = grid_sort(sites[by_id], dim)
+    order = by_id[order_local]
+    s_sorted = sites[order]
+    id_sorted = ids[order]
+    nbr, _ = knn(s_sorted, None, K, key=id_sorted, nthreads=nthreads)
+    tk = tk or tet_k(n, len(tets))
+    cent = tet_centroids(verts, tets)
+    cand, _ = knn(s_sorted, cent, tk, key=id_sorted, exclude_self=False, nthreads=nthreads)
+    r = tet_cell(s_sorted, nbr, verts, tets, cand, mode=mode, nthreads=nthreads)
+    new = lloyd_update(s_sorted, r["vol"], r["mom"], mode=mode)
+    return dict(order=order, ids=id_sorted, sites=s_sorted, cell_start=cs, dim=dim, nbr=nbr, tk=tk,
+                centroids=cent, cand=cand, vol=r["vol"], mom=r["mom"], hist=r["hist"],
+                counters=r["counters"], new_sites=new)
+
+
+# ---------------------------------------------------------------------------
+# Host build of the reference's own kernels.
+# ---------------------------------------------------------------------------
+_refs: dict = {}
+
+
+def ref_available(k: int) -> bool:
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_make_ref", HERE / "make_ref.py")
+    mr = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mr)
+    p = mr.lib_path(k)
+    if not p.exists():
+        try:
+            mr.build([k])
+        except Exception:
+            return False
+    return p.exists()
+
+
+def ref_lib(k: int):
+    """The reference's kernels compiled for the host with site-K = k."""
+    if k not in _refs:
+        if not ref_available(k):
+            raise FileNotFoundError(f"reference host build for K={k} is not available")
+        L = C.CDLL(str(HERE / "_ref" / f"libref_host_k{k}.so"))
+        vp, i, ll = C.c_void_p, C.c_int, C.c_longlong
+        L.ref_site_k.restype = i
+        L.ref_tet_cell.argtypes = [vp, i, vp, vp, i, vp, i, vp, i, ll, ll, vp, vp, vp, i]
+        L.ref_cell_tet.argtypes = [vp, i, vp, vp, i, vp, i, vp, i, i, i, ll, ll, vp, vp, vp, i]
+        L.ref_new_site.argtypes = [vp, i, vp, vp]
+        L.ref_tet_centroids.argtypes = [vp, i, vp, i, vp]
+        L.ref_knn_brute.argtypes = [vp, i, vp, i, i, i, vp, i]
+        L.ref_knn_grid.argtypes = [vp, i, vp, vp, vp, i]
+        L.ref_knn_grid.restype = i
+        _refs[k] = L
+    return _refs[k]
+
+
+def ref_tet_cell(sites, nbr, verts, tets, cand, pairs=None, nthreads: int = 0):
+    """Reference tet-cell kernel (float, shipped).  pairs=(begin,end) of the
+    tet-major pair space; returns vol (n,), bary (n,3) float32, status."""
+    sites, nbr, verts, tets, cand = _f32(sites), _i32(nbr), _f32(verts), _i32(tets), _i32(cand)
+    n, K = nbr.shape
+    nt, tk = cand.shape
+    L = ref_lib(K)
+    b, e = pairs if pairs is not None else (0, nt * tk)
+    vol = np.zeros(n, np.float32)
+    bary = np.zeros((n, 3), np.float32)
+    st = np.full(nt * tk, -1, np.int32)
+    L.ref_tet_cell(_p(sites), n, _p(nbr), _p(verts), len(verts), _p(tets), nt, _p(cand), tk, b, e,
+                   _p(vol), _p(bary), _p(st), nthreads)
+    return vol, bary, st.reshape(nt, tk)
+
+
+def ref_cell_tet(sites, nbr, verts, tets, cand, sites_range=None, pairs=None, nthreads: int = 0):
+    sites, nbr, verts, tets, cand = _f32(sites), _i32(nbr), _f32(verts), _i32(tets), _i32(cand)
+    n, K = nbr.shape
+    nt, tk = cand.shape
+    L = ref_lib(K)
+    sb, se = sites_range if sites_range is not None else (0, n)
+    b, e = pairs if pairs is not None else (0, nt * tk)
+    vol = np.zeros(n, np.float32)
+    bary = np.zeros((n, 3), np.float32)
+    st = np.full(nt * tk, -1, np.int32)
+    L.ref_cell_tet(_p(sites), n, _p(nbr), _p(verts), len(verts), _p(tets), nt, _p(cand), tk, sb, se, b, e,
+                   _p(vol), _p(bary), _p(st), nthreads)
+    return vol, bary, st.reshape(nt, tk)
+
+
+def ref_tet_centroids(verts, tets, k: int = 90):
+    verts, tets = _f32(verts), _i32(tets)
+    out = np.empty((len(tets), 3), np.float32)
+    ref_lib(k).ref_tet_centroids(_p(verts), len(verts), _p(tets), len(tets), _p(out))
+    return out
+
+
+def ref_knn_brute(ref, qry, k: int, q_range=None, nthreads: int = 0, site_k: int = 90):
+    ref, qry = _f32(ref), _f32(qry)
+    qb, qe = q_range if q_range is not None else (0, len(qry))
+    out = np.empty((qe - qb, k), np.int32)
+    ref_lib(site_k).ref_knn_brute(_p(ref), len(ref), _p(qry), qb, qe, k, _p(out), nthreads)
+    return out
+
+
+def ref_knn_grid(pts, k: int, nthreads: int = 0):
+    """Reference grid kNN on the host: (perm sorted->original, sorted points, knn in sorted space)."""
+    pts = _f32(pts)
+    n = len(pts)
+    perm = np.empty(n, np.uint32)
+    srt = np.empty((n, 3), np.float32)
+    kn = np.empty((n, k), np.uint32)
+    rc = ref_lib(k).ref_knn_grid(_p(pts), n, _p(perm), _p(srt), _p(kn), nthreads)
+    if rc != 0:
+        raise ValueError("reference grid kNN needs at least ~12.7k points (grid side >= 16)")
+    return perm.astype(np.int64), srt, kn.astype(np.int64)
