@@ -1,0 +1,140 @@
+// Shared device helpers and internal interfaces of the GB300 clipped-Voronoi
+// engine.  Device code targets sm_103a only.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+namespace vgb {
+
+// Pair status values; identical to the reference's enum Status
+// (voronoi_defs.h:4-12) so that histograms read the same.
+enum PairStatus : int {
+  ST_TRIANGLE_OVERFLOW = 0,
+  ST_VERTEX_OVERFLOW = 1,
+  ST_INCONSISTENT_BOUNDARY = 2,
+  ST_SECURITY_RADIUS_NOT_REACHED = 3,
+  ST_SUCCESS = 4,
+  ST_NEEDS_EXACT_PREDICATES = 5,
+  ST_NO_INTERSECTION = 6,
+};
+
+// Counters written by the clip kernel (one slot each, 64-bit).
+enum StatSlot : int {
+  STAT_CANDIDATES = 0,       // (tet, site) candidate pairs examined
+  STAT_CULLED = 1,           // pairs rejected by the one-plane separation test
+  STAT_CLIPPED = 2,          // pairs run through the full clip
+  STAT_EMPTY = 3,            // clipped pairs that came out empty
+  STAT_CONTRIB = 4,          // pairs that contributed volume
+  STAT_SECURITY_MISS = 5,    // contributing pairs whose K-list never reached the security radius
+  STAT_TRI_OVERFLOW = 6,     // pairs dropped because the cell exceeded its triangle capacity
+  STAT_BOUNDARY_FAIL = 7,    // pairs dropped because the cavity boundary was not one loop
+  STAT_PLANES = 8,           // bisector planes applied
+  STAT_CLIPS = 9,            // planes that removed at least one vertex
+  STAT_FINAL_VERTICES = 10,  // cell vertices decomposed into sub-tets
+  STAT_CONFLICT_TESTS = 11,  // vertex-vs-plane tests of the clip loop
+  STAT_CULL_TESTS = 12,      // tet-vs-plane tests of the separation pass
+  STAT_NEW_VERTICES = 13,    // vertices created by clipping
+  STAT_COUNT = 16
+};
+
+constexpr int WARP = 32;
+constexpr int MAX_SITE_K = 128;   // largest supported site-kNN K
+constexpr int MAX_TET_K = 128;    // largest supported candidates per tet
+constexpr int TRI_SLOTS = 4;      // triangles per lane in the clip kernel
+constexpr int MAX_TRI = WARP * TRI_SLOTS;
+
+// Grid of the reference (knearests.cu:19-27, :243): dim^3 cells over
+// [0,1000]^3, a point's cell is floor(p * dim / 1000) clamped, in float.
+__host__ __device__ inline int grid_axis(float p, int dim) {
+#ifdef __CUDA_ARCH__
+  float f = floorf(__fdiv_rn(__fmul_rn(p, (float)dim), 1000.f));
+#else
+  float f = floorf((p * (float)dim) / 1000.f);
+#endif
+  int i = (int)f;
+  return i < 0 ? 0 : (i > dim - 1 ? dim - 1 : i);
+}
+
+__host__ __device__ inline int grid_cell(float x, float y, float z, int dim) {
+  return grid_axis(x, dim) + dim * (grid_axis(y, dim) + dim * grid_axis(z, dim));
+}
+
+// Squared distance as the reference's kernels evaluate it after nvcc's FMA
+// contraction (knearests.cu:122, knncuda.cu:79): fma(dz,dz, fma(dy,dy, dx*dx)),
+// with d = candidate - query.
+__device__ __forceinline__ float dist2(float4 q, float4 p) {
+  float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y), dz = __fsub_rn(p.z, q.z);
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+__device__ __forceinline__ int site_id(float4 p) { return __float_as_int(p.w); }
+
+// Per-site moments in double: x = volume, (y, z, w) = first moment.  One
+// 32-byte aligned record per site.
+struct __align__(32) dmom4 {
+  double x, y, z, w;
+};
+__host__ __device__ inline dmom4 make_dmom4(double x, double y, double z, double w) {
+  dmom4 r;
+  r.x = x; r.y = y; r.z = z; r.w = w;
+  return r;
+}
+
+// --- host-side plumbing ----------------------------------------------------
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define VGB_CUDA_TRY(expr)                                                              \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::vgb::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
+      return -2;                                                                        \
+    }                                                                                   \
+  } while (0)
+
+// --- internal launchers (all asynchronous on `st`) -------------------------
+
+// Exclusive scan of n ints (in may alias out).  tmp must hold scan_tmp_ints(n).
+size_t scan_tmp_ints(long long n);
+int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t st);
+
+// Grid sort of n sites (float4 x,y,z,id) by (cell, id).
+//   cell_start: dim^3 + 1 ints; cell_fill, site_cell: scratch (dim^3, n ints).
+//   scan_tmp: scan_tmp_ints(dim^3 + 1) ints.
+int grid_sort(const float4* in, float4* out, int n, int dim, int* cell_start, int* cell_fill, int* site_cell,
+              int* scan_tmp, cudaStream_t st);
+
+// K nearest sorted sites of every sorted site (self excluded) or of every tet
+// centroid, ordered by (distance, id).  Output rows are sorted-space indices.
+int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, unsigned* out, cudaStream_t st);
+int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const float4* verts,
+                      const int4* tets, int n_tet, int k, unsigned* out, cudaStream_t st);
+
+// Site-major lists of candidate tets: for each site, the tets whose candidate
+// row holds it.  start: n+1 ints, fill: n ints scratch, list: n_tet*tk ints.
+int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* start, int* fill, int* list,
+                       int* scan_tmp, cudaStream_t st);
+
+// Tet-cell clipping of every candidate pair, site-major, per-site moments in
+// double relative to the site: mom[s] = (vol, mx, my, mz).
+int clip_tet_cell(const float4* sites, int n, const unsigned* knn, int k, const float4* verts, const int4* tets,
+                  const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
+                  cudaStream_t st);
+
+// Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
+// atomics into per-site sums (the plain form).  mom_f: n float4 (vol, m).
+int clip_tet_cell_plain(const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
+                        const int4* tets, int n_tet, const unsigned* cand, int tk, float4* mom_f,
+                        unsigned long long* stats, cudaStream_t st);
+
+// One-time kernel attributes / launch shapes; call outside stream capture.
+int knn_prepare();
+int clip_prepare();
+
+
+}  // namespace vgb

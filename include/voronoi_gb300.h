@@ -1,0 +1,182 @@
+/*
+ * voronoi_gb300.h -- C ABI of the GB300 clipped 3D Voronoi / Lloyd engine.
+ *
+ * Plain pointers and sizes only.  Coordinates are float32 in [0,1000]^3 (the
+ * reference's convention: meshes are normalised by load_tet,
+ * test_voronoi.cu:103-117, and sites are given in the same frame).  Tets are
+ * four 0-based vertex indices, positively oriented.  All calls are made from
+ * one host thread per engine; device work runs on the engine's own stream.
+ *
+ * Every function returns VGB_OK (0) or a negative error code; the message of
+ * the last error on the calling thread is vgb_last_error().
+ *
+ * This header replaces, for the hot path, the reference's entry point
+ * compute_clipped_voro_diagram_GPU (voronoi.h:78-84, voronoi.cu:925-1188):
+ * vgb_clipped_voro_diagram below has the same argument meaning, and
+ * include/voronoi.h wraps it with the reference's C++ signature.  The grid
+ * kNN calls kn_* of knearests.h (knearests.h:20-27) are in include/knearests.h.
+ */
+#ifndef VORONOI_GB300_H
+#define VORONOI_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VGB_OK 0
+#define VGB_ERR_INVALID (-1) /* bad argument or size                     */
+#define VGB_ERR_CUDA (-2)    /* CUDA runtime error (see vgb_last_error) */
+#define VGB_ERR_NOMEM (-3)   /* device or host allocation failed         */
+#define VGB_ERR_STATE (-4)   /* call out of order (e.g. no sites yet)    */
+
+/* Pair status values, identical to the reference's enum Status
+ * (voronoi_defs.h:4-12). */
+enum vgb_pair_status {
+  VGB_TRIANGLE_OVERFLOW = 0,
+  VGB_VERTEX_OVERFLOW = 1,
+  VGB_INCONSISTENT_BOUNDARY = 2,
+  VGB_SECURITY_RADIUS_NOT_REACHED = 3,
+  VGB_SUCCESS = 4,
+  VGB_NEEDS_EXACT_PREDICATES = 5,
+  VGB_NO_INTERSECTION = 6
+};
+
+/* Counters of the last pass (vgb_engine_get_stats). */
+enum vgb_stat {
+  VGB_STAT_CANDIDATES = 0,      /* (tet, site) candidate pairs examined              */
+  VGB_STAT_CULLED = 1,          /* rejected by the one-plane separation test          */
+  VGB_STAT_CLIPPED = 2,         /* run through the full clip                          */
+  VGB_STAT_EMPTY = 3,           /* clipped to nothing                                 */
+  VGB_STAT_CONTRIB = 4,         /* contributed volume                                 */
+  VGB_STAT_SECURITY_MISS = 5,   /* contributed without reaching the security radius   */
+  VGB_STAT_TRI_OVERFLOW = 6,    /* dropped: more cell vertices than the capacity      */
+  VGB_STAT_BOUNDARY_FAIL = 7,   /* dropped: cavity boundary not one loop              */
+  VGB_STAT_PLANES = 8,          /* bisector planes applied                            */
+  VGB_STAT_CLIPS = 9,           /* planes that removed a vertex                       */
+  VGB_STAT_FINAL_VERTICES = 10, /* cell vertices decomposed into sub-tets             */
+  VGB_STAT_CONFLICT_TESTS = 11, /* vertex-vs-plane tests while clipping               */
+  VGB_STAT_CULL_TESTS = 12,     /* tet-vs-plane tests of the separation pass          */
+  VGB_STAT_NEW_VERTICES = 13,   /* vertices created by clipping                       */
+  VGB_STAT_COUNT = 16
+};
+
+/* Clip kernels. */
+#define VGB_METHOD_SITE_MAJOR 0 /* warp per site, FP64 per-site moments (default) */
+#define VGB_METHOD_PLAIN 1      /* thread per (tet, site) pair, float atomics      */
+
+/* Buffers readable with vgb_engine_copy_buffer. */
+enum vgb_buffer {
+  VGB_BUF_SITES = 0,      /* float4[n]: x, y, z, original id (int bits), grid order */
+  VGB_BUF_KNN = 1,        /* uint32[n][site_k]: neighbours in grid order           */
+  VGB_BUF_CAND = 2,       /* uint32[n_tet][tet_k]: candidate sites per tet          */
+  VGB_BUF_CELL_START = 3, /* int32[grid_dim^3 + 1]                                  */
+  VGB_BUF_SITE_START = 4, /* int32[n + 1]: start of each site's candidate tets      */
+  VGB_BUF_SITE_TETS = 5,  /* int32[n_tet * tet_k]                                   */
+  VGB_BUF_MOMENTS = 6     /* double4[n]: volume, first moment (absolute)            */
+};
+
+typedef struct vgb_config {
+  int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9)   */
+  int tet_k;    /* candidate sites per tet; 0 = the reference heuristic (voronoi.cu:936) */
+  int grid_dim; /* site grid side; 0 = round((n/3.1)^(1/3)) (knearests.cu:243)           */
+  int method;   /* VGB_METHOD_*                                                          */
+  int use_graph;/* capture one Lloyd iteration as a CUDA graph and replay it             */
+  int device;   /* CUDA device ordinal                                                   */
+} vgb_config;
+
+typedef struct vgb_engine vgb_engine;
+
+/* Defaults: site_k 90, tet_k 0, grid_dim 0, site-major, graphs on, device 0. */
+void vgb_config_init(vgb_config* cfg);
+
+/* One-line description of a CUDA device (name, SMs, memory) into buf. */
+int vgb_device_describe(int device, char* buf, int len);
+
+/* Message of the last error on this thread ("" if none). */
+const char* vgb_last_error(void);
+
+/* max(10*ceil(8*log10(7*n_site/n_tet + 1)), 20), or `preferred` when non-zero
+ * (voronoi.cu:936), clamped to [1, n_site]. */
+int vgb_tet_k(int n_site, int n_tet, int preferred);
+
+/* Grid side for n sites: max(1, round((n/3.1)^(1/3))) (knearests.cu:243). */
+int vgb_grid_dim(int n_site);
+
+/* Create an engine: uploads the mesh (verts: n_vert x 3, tets: n_tet x 4) and
+ * the sites (n_site x 3, original order; site i gets id i) and allocates every
+ * buffer of the path.  Requires site_k < n_site. */
+int vgb_engine_create(vgb_engine** out, const vgb_config* cfg, const float* verts, int n_vert, const int* tets,
+                      int n_tet, const float* sites, int n_site);
+int vgb_engine_destroy(vgb_engine* e);
+
+/* Replace the sites (host, n_site x 3, original order, ids 0..n-1). */
+int vgb_engine_set_sites(vgb_engine* e, const float* sites);
+
+/* Run n_iter passes of the path: grid sort, site kNN, tet candidates, clip,
+ * per-site moments; with update != 0 each pass ends with the Lloyd update.
+ * Asynchronous on the engine stream. */
+int vgb_engine_iterate(vgb_engine* e, int n_iter, int update);
+
+/* Host-buffer pass: copy sites in (n_site x 3, grid order of the engine, ids
+ * kept), run one Lloyd iteration, copy the new sites out (grid order).
+ * Synchronous.  The end-to-end form of one step. */
+int vgb_engine_step_host(vgb_engine* e, const float* sites_in, float* sites_out);
+
+int vgb_engine_sync(vgb_engine* e);
+
+/* Sites in the engine's grid order: xyz (n x 3) and, if ids != NULL, the
+ * original id of each. */
+int vgb_engine_get_sites(vgb_engine* e, float* xyz, int* ids);
+
+/* Sites in original order (n x 3). */
+int vgb_engine_get_sites_original(vgb_engine* e, float* xyz);
+
+/* Per-site volume and absolute first moment (sum vol * barycentre) of the last
+ * pass, in grid order (vol: n, mom: n x 3; either may be NULL). */
+int vgb_engine_get_moments(vgb_engine* e, double* vol, double* mom);
+
+/* Counters of the last pass: out[VGB_STAT_COUNT]. */
+int vgb_engine_get_stats(vgb_engine* e, unsigned long long* out);
+
+/* Copy a device buffer (enum vgb_buffer) to host; bytes must equal its size. */
+int vgb_engine_copy_buffer(vgb_engine* e, int which, void* host, size_t bytes);
+size_t vgb_engine_buffer_bytes(vgb_engine* e, int which);
+
+/* Turn CUDA-graph replay of the iteration on or off. */
+int vgb_engine_set_graph(vgb_engine* e, int use_graph);
+
+/* Page-locked host buffers for vgb_engine_step_host (cudaMallocHost/FreeHost). */
+void* vgb_host_alloc(size_t bytes);
+void vgb_host_free(void* p);
+
+/* Sizes the engine settled on. */
+int vgb_engine_info(vgb_engine* e, int* n_site, int* n_tet, int* site_k, int* tet_k, int* grid_dim);
+
+/* Device time in ms of the phases of the last non-graph pass:
+ * [0] grid sort, [1] site kNN, [2] tet candidates, [3] site-major candidate
+ * lists, [4] clip, [5] moments + update. */
+#define VGB_PHASES 6
+int vgb_engine_phase_ms(vgb_engine* e, float* ms);
+
+/* Run n_iter passes like vgb_engine_iterate between two CUDA events recorded
+ * on the engine stream, wait for them, and return the elapsed device time. */
+int vgb_engine_time_iterate(vgb_engine* e, int n_iter, int update, float* ms);
+
+/* The drop-in Lloyd driver (compute_clipped_voro_diagram_GPU,
+ * voronoi.cu:925-1188).  site: n_site x 3, AoS when site_is_transposed == 0
+ * (updated in place and, like the reference's grid-kNN path, left in grid
+ * order), SoA (3 rows of n_site) otherwise (original order kept).
+ * nb_Lloyd_iter iterations; preferred_tet_k = 0 uses the heuristic; site_k = 0
+ * uses 90.  With write_files != 0, appends to record.csv and writes
+ * iter_<i>.xyz in the working directory like the reference. */
+int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const int* indices, int n_tet, float* site,
+                             int n_site, int site_is_transposed, int nb_Lloyd_iter, int preferred_tet_k,
+                             int site_k, int write_files);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VORONOI_GB300_H */

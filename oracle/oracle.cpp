@@ -494,6 +494,83 @@ void orc_knn(const float* ref, int n, const int* key, const float* qry, int nq, 
   }
 }
 
+// Same selection as orc_knn, accelerated by a uniform grid of `dim`^3 cells
+// over [0,1000]^3 (the reference's cell rule): rings of cells around the
+// query's cell until the k-th distance is below the distance to every
+// unvisited cell.  Results are identical to the brute force.
+void orc_knn_grid(const float* ref, int n, const int* key, const float* qry, int nq, int K, int exclude_self,
+                  int dim, int* out_idx, int nthreads) {
+  long long nc = (long long)dim * dim * dim;
+  std::vector<int> cell(n), start(nc + 1, 0), order(n);
+  for (int i = 0; i < n; ++i) {
+    cell[i] = cell_of(ref[3 * i], ref[3 * i + 1], ref[3 * i + 2], dim);
+    start[cell[i] + 1]++;
+  }
+  for (long long c = 0; c < nc; ++c) start[c + 1] += start[c];
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < n; ++i) order[fill[cell[i]]++] = i;
+  }
+  const double h = 1000.0 / dim;
+  const double margin = 0.01;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+  {
+    std::vector<std::pair<float, long long>> best;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (int q = 0; q < nq; ++q) {
+      best.clear();
+      float qx = qry[3 * q], qy = qry[3 * q + 1], qz = qry[3 * q + 2];
+      int ci = cell_of(qx, 0.f, 0.f, dim) % dim;
+      int cj = cell_of(0.f, qy, 0.f, dim) / dim % dim;
+      int ck = cell_of(0.f, 0.f, qz, dim) / dim / dim;
+      auto consider = [&](int i) {
+        if (exclude_self && i == q) return;
+        float d = dist2(qx, qy, qz, ref[3 * i], ref[3 * i + 1], ref[3 * i + 2]);
+        long long k = key ? key[i] : i;
+        if ((int)best.size() == K) {
+          const auto& w = best.back();
+          if (d > w.first || (d == w.first && k > (w.second >> 32))) return;
+        }
+        std::pair<float, long long> e(d, (k << 32) | (unsigned)i);
+        best.insert(std::upper_bound(best.begin(), best.end(), e), e);
+        if ((int)best.size() > K) best.pop_back();
+      };
+      for (int r = 0; r <= dim; ++r) {
+        if ((int)best.size() == K && r > 0) {
+          double L = 1e300;
+          if (ci - r >= 0) L = std::min(L, qx - (ci - r + 1) * h);
+          if (ci + r <= dim - 1) L = std::min(L, (ci + r) * h - qx);
+          if (cj - r >= 0) L = std::min(L, qy - (cj - r + 1) * h);
+          if (cj + r <= dim - 1) L = std::min(L, (cj + r) * h - qy);
+          if (ck - r >= 0) L = std::min(L, qz - (ck - r + 1) * h);
+          if (ck + r <= dim - 1) L = std::min(L, (ck + r) * h - qz);
+          L -= margin;
+          if (L > 0 && (double)best.back().first < L * L) break;
+        }
+        for (int k = ck - r; k <= ck + r; ++k) {
+          if (k < 0 || k >= dim) continue;
+          for (int j = cj - r; j <= cj + r; ++j) {
+            if (j < 0 || j >= dim) continue;
+            bool edge = (k == ck - r || k == ck + r || j == cj - r || j == cj + r);
+            for (int i = ci - r; i <= ci + r; i += (edge || r == 0) ? 1 : 2 * r) {
+              if (i < 0 || i >= dim) continue;
+              long long c = i + (long long)dim * (j + (long long)dim * k);
+              for (int p = start[c]; p < start[c + 1]; ++p) consider(order[p]);
+            }
+          }
+        }
+      }
+      for (int j = 0; j < K; ++j)
+        out_idx[(long long)q * K + j] = j < (int)best.size() ? (int)(best[j].second & 0xffffffffLL) : -1;
+    }
+  }
+}
+
 // Tet centroids, float, summed a, b, c, d from zero then scaled by 0.25f
 // (voronoi.cu:751-779).
 void orc_tet_centroids(const float* verts, const int* tets, int nt, float* out) {

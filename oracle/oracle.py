@@ -62,6 +62,7 @@ def lib():
         L.orc_cell_of.restype = i
         L.orc_grid_sort.argtypes = [vp, i, i, vp, vp]
         L.orc_knn.argtypes = [vp, i, vp, vp, i, i, i, vp, vp, i]
+        L.orc_knn_grid.argtypes = [vp, i, vp, vp, i, i, i, i, vp, i]
         L.orc_tet_centroids.argtypes = [vp, vp, i, vp]
         L.orc_tet_k.argtypes = [i, i, i]
         L.orc_tet_k.restype = i
@@ -103,6 +104,23 @@ def knn(ref, qry=None, k: int = 64, key=None, exclude_self: bool | None = None, 
     dd = np.empty((nq, k), np.float32)
     lib().orc_knn(_p(ref), len(ref), _p(key), _p(qry), nq, k, int(bool(exclude_self)), _p(idx), _p(dd), nthreads)
     return idx, dd
+
+
+def knn_grid(ref, qry=None, k: int = 64, key=None, exclude_self: bool | None = None, dim: int = 0,
+             nthreads: int = 0):
+    """Same result as knn(), through a uniform grid (for large point sets)."""
+    ref = _f32(ref)
+    if qry is None:
+        qry = ref
+        if exclude_self is None:
+            exclude_self = True
+    qry = _f32(qry)
+    key = _i32(key) if key is not None else None
+    dim = dim or grid_dim(len(ref))
+    idx = np.empty((len(qry), k), np.int32)
+    lib().orc_knn_grid(_p(ref), len(ref), _p(key), _p(qry), len(qry), k, int(bool(exclude_self)), dim, _p(idx),
+                       nthreads)
+    return idx
 
 
 def tet_centroids(verts, tets):

@@ -253,4 +253,81 @@ int ref_knn_grid(const float* pts, int n, unsigned* perm, float* sorted, unsigne
   return 0;
 }
 
+// --- timed samples for the CPU baseline --------------------------------------
+// A prepared problem keeps the reference layouts so that only kernel work is
+// timed.  Pair ids are tet * tet_k + slot (the reference's thread id).
+struct RefProblem {
+  const float* sites;
+  int n_site;
+  const int* knn;
+  int n_vert, n_tet, tet_k;
+  TetSoA mesh;
+  std::vector<VoronoiCell> cells;
+  std::vector<Status> st;
+  std::vector<float> vol, bary;
+  RefProblem(const float* s, int n, const int* k, const float* v, int nv, const int* t, int nt, const int* c, int tk)
+      : sites(s), n_site(n), knn(k), n_vert(nv), n_tet(nt), tet_k(tk), mesh(v, nv, t, nt, c, tk),
+        cells((size_t)n), st((size_t)nt * tk, security_radius_not_reached), vol((size_t)n, 0.f),
+        bary(3 * (size_t)n, 0.f) {
+    std::memset((void*)cells.data(), 0, sizeof(VoronoiCell) * (size_t)n);
+  }
+};
+
+void* ref_prepare(const float* sites, int n_site, const int* knn, const float* verts, int n_vert, const int* tets,
+                  int n_tet, const int* cand, int tet_k) {
+  return new RefProblem(sites, n_site, knn, verts, n_vert, tets, n_tet, cand, tet_k);
+}
+
+void ref_release(void* h) { delete static_cast<RefProblem*>(h); }
+
+double ref_time_tet_cell(void* h, const long long* pairs, long long np, int nthreads) {
+  RefProblem& P = *static_cast<RefProblem*>(h);
+  set_threads(nthreads);
+  double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long long i = 0; i < np; ++i) {
+    set_thread(pairs[i], 1);
+    clipped_voro_cell_test_GPU_param_tet(P.sites, P.n_site, 0, P.knn, 0, P.mesh.vert.data(), P.n_vert,
+                                         (size_t)P.n_vert, P.mesh.idx.data(), P.n_tet, (size_t)P.n_tet,
+                                         P.mesh.cand.data(), (size_t)P.n_tet, P.tet_k, P.st.data(), nullptr,
+                                         P.bary.data(), 0, P.vol.data());
+  }
+  return omp_get_wtime() - t0;
+}
+
+double ref_time_cells(void* h, const int* sites, int ns, int nthreads) {
+  RefProblem& P = *static_cast<RefProblem*>(h);
+  set_threads(nthreads);
+  double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i < ns; ++i) {
+    set_thread(sites[i], 1);
+    voro_cell_test_GPU_param(P.sites, P.n_site, 0, P.knn, 0, P.cells.data());
+  }
+  return omp_get_wtime() - t0;
+}
+
+double ref_time_cell_tet(void* h, const long long* pairs, long long np, int nthreads) {
+  RefProblem& P = *static_cast<RefProblem*>(h);
+  set_threads(nthreads);
+  double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long long i = 0; i < np; ++i) {
+    set_thread(pairs[i], 1);
+    clipped_voro_cell_test_GPU_param(P.mesh.vert.data(), P.n_vert, (size_t)P.n_vert, P.mesh.idx.data(), P.n_tet,
+                                     (size_t)P.n_tet, P.mesh.cand.data(), (size_t)P.n_tet, P.tet_k, P.st.data(),
+                                     P.cells.data(), P.bary.data(), 0, P.vol.data());
+  }
+  return omp_get_wtime() - t0;
+}
+
+// Grid kNN of the reference (kn_prepare + kn_solve on the host), timed.
+double ref_time_knn_grid(const float* pts, int n, unsigned* perm, float* sorted, unsigned* knn, int nthreads) {
+  double t0 = omp_get_wtime();
+  if (ref_knn_grid(pts, n, perm, sorted, knn, nthreads) != 0) return -1.0;
+  return omp_get_wtime() - t0;
+}
+
+int ref_max_threads() { return omp_get_max_threads(); }
+
 }  // extern "C"
