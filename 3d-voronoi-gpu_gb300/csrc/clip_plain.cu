@@ -131,8 +131,10 @@ struct PlainCell {
     int cir = first;
     do {
       if (nt + 1 >= PL_MAXT) { status = ST_TRIANGLE_OVERFLOW; return; }
-      T(nt++) = mk(cur, cir, B(cir));
-      cir = B(cir);
+      int nx = B(cir);
+      if (nx == PL_END) { status = ST_INCONSISTENT_BOUNDARY; return; }  // open boundary chain
+      T(nt++) = mk(cur, cir, nx);
+      cir = nx;
     } while (cir != first);
   }
 };

@@ -122,7 +122,7 @@ struct Cell {
   int cap_p, cap_t;
   V4<R> pl[CAP];
   uint8_t tr[CAP][3];
-  uint8_t bnext[CAP];
+  uint8_t bnext[CAP + 1];  // one more slot: the end marker itself is a valid index
   int nv = 0, nt = 0, nr = 0;
   int first = END;
   V4<R> seed;
@@ -246,7 +246,7 @@ struct Cell {
   // removed triangles are absorbed one by one while the border stays a
   // simple loop (voronoi.cu:391-441).
   void cavity_boundary() {
-    for (int i = 0; i < CAP; ++i) bnext[i] = END;
+    for (int i = 0; i <= CAP; ++i) bnext[i] = END;
     first = END;
     int iters = 0;
     int t = nt;
