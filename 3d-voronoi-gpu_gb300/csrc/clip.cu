@@ -20,9 +20,12 @@
 //     is one 4-term dot product per vertex and a ballot;
 //   * the cavity boundary is found in parallel: a directed edge of a removed
 //     triangle is on the boundary when no other removed triangle holds its
-//     twin; each boundary edge (a, b) becomes the new triangle (plane, a, b)
+//     twin -- one lane per edge and a __match_any_sync on the undirected edge
+//     key; each boundary edge (a, b) becomes the new triangle (plane, a, b)
 //     -- the same triangles the reference's boundary walk produces
-//     (voronoi.cu:391-441, 479-485), in a different order;
+//     (voronoi.cu:391-441, 479-485), in a different order.  Surviving
+//     triangles keep their slots; new ones fill the freed slots and the
+//     receiving lane computes the new vertex;
 //   * moments are taken from the mean of the cell's vertices instead of the
 //     site (any apex gives the same sums; an inside apex avoids cancellation),
 //     with the edge feet computed from the edge direction n_p x n_q, which is
@@ -44,8 +47,6 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct ClipWarpSmem {
   float4 plane[4 + MAX_SITE_K];  // 0..3 tet faces, 4+j bisector of neighbour j
-  float4 vstage[MAX_TRI];        // compaction staging: vertex x, y, z, |v|^2
-  unsigned tstage[MAX_TRI];      // compaction staging: packed triangles
   unsigned conf[MAX_TRI];        // removed triangles of the current clip
   unsigned bedge[MAX_TRI];       // boundary edges (a | b << 8) of the current clip
 };
@@ -200,32 +201,36 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
         if (lane == 1) S.plane[1] = face_plane(a, c, d);
         if (lane == 2) S.plane[2] = face_plane(b, a, d);
         if (lane == 3) S.plane[3] = face_plane(a, b, c);
-        // initial cell: the tet's corners as triangles of their three faces
+        // initial cell: the tet's corners as triangles of their three faces.
+        // Slot (k, lane) holds one triangle; vm[k] marks the live slots.
         unsigned tri[TRI_SLOTS];
         float vx[TRI_SLOTS], vy[TRI_SLOTS], vz[TRI_SLOTS], vw[TRI_SLOTS];
+        unsigned vm[TRI_SLOTS];
 #pragma unroll
-        for (int k = 0; k < TRI_SLOTS; ++k) { tri[k] = 0; vx[k] = vy[k] = vz[k] = vw[k] = 0.f; }
+        for (int k = 0; k < TRI_SLOTS; ++k) { tri[k] = 0; vx[k] = vy[k] = vz[k] = vw[k] = 0.f; vm[k] = 0u; }
         {
           float4 p = lane == 0 ? a : lane == 1 ? d : lane == 2 ? c : b;
           tri[0] = lane == 0 ? pack_tri(1, 3, 2) : lane == 1 ? pack_tri(0, 1, 2) : lane == 2 ? pack_tri(0, 3, 1)
                                                                                                : pack_tri(0, 2, 3);
           vx[0] = p.x; vy[0] = p.y; vz[0] = p.z; vw[0] = p.x * p.x + p.y * p.y + p.z * p.z;
+          vm[0] = 0xfu;
         }
         int nt = 4;
         float r2 = warp_max(lane < 4 ? vw[0] : 0.f);
         __syncwarp();
         int state = 0;  // 0 running, 1 security radius reached, 2 empty, 3 dropped (capacity/boundary)
-        int j = 0;
-        for (; j < K; ++j) {
+        for (int j = 0; j < K; ++j) {
           const float4 P = S.plane[4 + j];
           unsigned m[TRI_SLOTS];
           int nconf = 0;
 #pragma unroll
           for (int k = 0; k < TRI_SLOTS; ++k) {
-            bool live = k * WARP + lane < nt;
-            bool cf = live && plane_eval(P, vx[k], vy[k], vz[k]) < 0.f;
-            m[k] = (k * WARP < nt) ? __ballot_sync(FULL, cf) : 0u;
-            nconf += __popc(m[k]);
+            m[k] = 0u;
+            if (vm[k]) {
+              bool cf = ((vm[k] >> lane) & 1u) && plane_eval(P, vx[k], vy[k], vz[k]) < 0.f;
+              m[k] = __ballot_sync(FULL, cf);
+              nconf += __popc(m[k]);
+            }
           }
           if (lane == 0) { c_planes++; c_conflict += (unsigned)nt; }
           if (nconf == 0) {
@@ -234,109 +239,116 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
           }
           if (nconf == nt) { state = 2; break; }
           if (lane == 0) c_clips++;
-          // removed triangles, compacted in index order
+          // removed triangles, compacted in slot order
           {
             int off = 0;
 #pragma unroll
             for (int k = 0; k < TRI_SLOTS; ++k) {
-              if (m[k] >> lane & 1u) S.conf[off + __popc(m[k] & lt_mask)] = tri[k];
+              if ((m[k] >> lane) & 1u) S.conf[off + __popc(m[k] & lt_mask)] = tri[k];
               off += __popc(m[k]);
             }
           }
           __syncwarp();
           const int R = nconf;
-          // boundary edges: (a -> b) of a removed triangle whose twin (b -> a)
-          // is in no removed triangle
+          // boundary edges: a directed edge (a -> b) of a removed triangle whose
+          // twin (b -> a) is in no removed triangle.  Each undirected edge of
+          // the removed region appears twice inside it, once on its border.
           int nb = 0;
           bool bad = false;
-          const unsigned pj = (unsigned)(4 + j);
-          for (int e0 = 0; e0 < 3 * R; e0 += WARP) {
-            const int e = e0 + lane;
-            bool isb = false;
+          if (3 * R <= WARP) {
+            const bool live = lane < 3 * R;
             unsigned ea = 0, eb = 0;
-            if (e < 3 * R) {
-              unsigned T = S.conf[e / 3];
-              int es = e % 3;
+            if (live) {
+              unsigned T = S.conf[lane / 3];
+              int es = lane % 3;
               ea = tri_at(T, es);
               eb = tri_at(T, (es + 1) % 3);
-              bool twin = false;
-              for (int q = 0; q < R; ++q) {
-                unsigned U = S.conf[q];
-                unsigned u0 = tri_at(U, 0), u1 = tri_at(U, 1), u2 = tri_at(U, 2);
-                twin |= (u0 == eb && u1 == ea) || (u1 == eb && u2 == ea) || (u2 == eb && u0 == ea);
-              }
-              isb = !twin;
             }
-            unsigned bm = __ballot_sync(FULL, isb);
-            if (isb) {
-              int r = nb + __popc(bm & lt_mask);
-              if (r < MAX_TRI) S.bedge[r] = ea | (eb << 8);
-            }
-            nb += __popc(bm);
-          }
-          const int nt2 = nt - R + nb;
-          if (nt2 > MAX_TRI || nb < 3) {
-            bad = true;
-          }
-          __syncwarp();
-          if (!bad) {
-            // each boundary vertex must start exactly one edge and end exactly one
-            for (int e = lane; e < nb; e += WARP) {
-              unsigned E = S.bedge[e];
-              int starts = 0, ends = 0;
-              for (int q = 0; q < nb; ++q) {
-                unsigned F = S.bedge[q];
-                starts += (F & 0xffu) == (E & 0xffu);
-                ends += (F >> 8) == (E >> 8);
+            // every lane takes part in each match (full-warp collectives)
+            const unsigned key = live ? (min(ea, eb) | (max(ea, eb) << 8)) : (0x10000u | lane);
+            const unsigned same = __match_any_sync(FULL, key);
+            const bool isb = live && __popc(same) == 1;
+            const unsigned bm = __ballot_sync(FULL, isb);
+            nb = __popc(bm);
+            // one outgoing and one incoming boundary edge per boundary vertex
+            const unsigned ka = isb ? ea : (0x20000u | lane), kb = isb ? eb : (0x30000u | lane);
+            const unsigned ga = __match_any_sync(FULL, ka);
+            const unsigned gb = __match_any_sync(FULL, kb);
+            const bool dup = isb && (__popc(ga) != 1 || __popc(gb) != 1);
+            bad = __any_sync(FULL, dup);
+            if (isb) S.bedge[__popc(bm & lt_mask)] = ea | (eb << 8);
+          } else {
+            for (int e0 = 0; e0 < 3 * R; e0 += WARP) {
+              const int e = e0 + lane;
+              bool isb = false;
+              unsigned ea = 0, eb = 0;
+              if (e < 3 * R) {
+                unsigned T = S.conf[e / 3];
+                int es = e % 3;
+                ea = tri_at(T, es);
+                eb = tri_at(T, (es + 1) % 3);
+                bool twin = false;
+                for (int q = 0; q < R; ++q) {
+                  unsigned U = S.conf[q];
+                  unsigned u0 = tri_at(U, 0), u1 = tri_at(U, 1), u2 = tri_at(U, 2);
+                  twin |= (u0 == eb && u1 == ea) || (u1 == eb && u2 == ea) || (u2 == eb && u0 == ea);
+                }
+                isb = !twin;
               }
-              if (starts != 1 || ends != 1) bad = true;
+              unsigned bm = __ballot_sync(FULL, isb);
+              if (isb) {
+                int r = nb + __popc(bm & lt_mask);
+                if (r < MAX_TRI) S.bedge[r] = ea | (eb << 8);
+              }
+              nb += __popc(bm);
+            }
+            __syncwarp();
+            if (nb <= MAX_TRI) {
+              for (int e = lane; e < nb; e += WARP) {
+                unsigned E = S.bedge[e];
+                int starts = 0, ends = 0;
+                for (int q = 0; q < nb; ++q) {
+                  unsigned F = S.bedge[q];
+                  starts += (F & 0xffu) == (E & 0xffu);
+                  ends += (F >> 8) == (E >> 8);
+                }
+                if (starts != 1 || ends != 1) bad = true;
+              }
             }
             bad = __any_sync(FULL, bad);
           }
-          if (bad) {
+          const int nt2 = nt - R + nb;
+          if (bad || nt2 > MAX_TRI || nb < 3) {
             if (lane == 0) { if (nt2 > MAX_TRI) c_overflow++; else c_boundary++; }
             state = 3;
             break;
           }
-          if (lane == 0) c_newv += (unsigned)nb;
-          // staging: kept triangles in index order, then the new fan
-          {
-            int off = 0;
-#pragma unroll
-            for (int k = 0; k < TRI_SLOTS; ++k) {
-              bool live = k * WARP + lane < nt;
-              bool keep = live && !(m[k] >> lane & 1u);
-              unsigned km = __ballot_sync(FULL, keep);
-              if (keep) {
-                int p = off + __popc(km & lt_mask);
-                S.tstage[p] = tri[k];
-                S.vstage[p] = make_float4(vx[k], vy[k], vz[k], vw[k]);
-              }
-              off += __popc(km);
-            }
-            const float4 Pj = P;
-            for (int e = lane; e < nb; e += WARP) {
-              unsigned E = S.bedge[e];
-              unsigned ea = E & 0xffu, eb = E >> 8;
-              float3 x = vertex_of(Pj, S.plane[ea], S.plane[eb]);
-              int p = nt - R + e;
-              S.tstage[p] = pack_tri(pj, ea, eb);
-              S.vstage[p] = make_float4(x.x, x.y, x.z, x.x * x.x + x.y * x.y + x.z * x.z);
-            }
-          }
           __syncwarp();
-          nt = nt2;
+          if (lane == 0) c_newv += (unsigned)nb;
+          // the new fan (plane, a, b) goes into free slots, in slot order; the
+          // receiving lane computes its vertex
+          const unsigned pj = (unsigned)(4 + j);
           float lm = 0.f;
+          int base = 0;
 #pragma unroll
           for (int k = 0; k < TRI_SLOTS; ++k) {
-            int i = k * WARP + lane;
-            if (i < nt) {
-              tri[k] = S.tstage[i];
-              float4 q = S.vstage[i];
-              vx[k] = q.x; vy[k] = q.y; vz[k] = q.z; vw[k] = q.w;
-              lm = fmaxf(lm, q.w);
+            const unsigned keep = vm[k] & ~m[k];
+            const unsigned freem = ~keep;
+            const int r = base + __popc(freem & lt_mask);
+            const bool recv = ((freem >> lane) & 1u) && r < nb;
+            if (recv) {
+              unsigned E = S.bedge[r];
+              unsigned ea = E & 0xffu, eb = E >> 8;
+              float3 x = vertex_of(P, S.plane[ea], S.plane[eb]);
+              tri[k] = pack_tri(pj, ea, eb);
+              vx[k] = x.x; vy[k] = x.y; vz[k] = x.z;
+              vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
             }
+            vm[k] = keep | __ballot_sync(FULL, recv);
+            base += __popc(freem);
+            if ((vm[k] >> lane) & 1u) lm = fmaxf(lm, vw[k]);
           }
+          nt = nt2;
           r2 = warp_max(lm);
           __syncwarp();
           if (2.f * P.w > 4.f * r2) { state = 1; break; }
@@ -352,13 +364,13 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
         float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
         for (int k = 0; k < TRI_SLOTS; ++k)
-          if (k * WARP + lane < nt) { sx += vx[k]; sy += vy[k]; sz += vz[k]; }
+          if ((vm[k] >> lane) & 1u) { sx += vx[k]; sy += vy[k]; sz += vz[k]; }
         const float inv = 1.f / (float)nt;
         const float cx = warp_sum(sx) * inv, cy = warp_sum(sy) * inv, cz = warp_sum(sz) * inv;
         float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
 #pragma unroll
         for (int k = 0; k < TRI_SLOTS; ++k) {
-          if (k * WARP + lane < nt) {
+          if ((vm[k] >> lane) & 1u) {
             unsigned T = tri[k];
             float4 q0 = S.plane[tri_at(T, 0)], q1 = S.plane[tri_at(T, 1)], q2 = S.plane[tri_at(T, 2)];
             // planes relative to the apex

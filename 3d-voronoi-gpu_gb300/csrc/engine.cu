@@ -37,6 +37,9 @@ struct vgb_engine {
   int* cell_fill = nullptr;
   int* site_cell = nullptr;
   int* scan_tmp = nullptr;
+  int* pos_of_id = nullptr;
+  int* tet_order = nullptr;       // tets sorted by centroid cell
+  int* tet_cell_start = nullptr;  // dim^3 + 1
   unsigned* knn = nullptr;
   unsigned* cand = nullptr;
   int* site_start = nullptr;
@@ -150,7 +153,7 @@ void free_engine(vgb_engine* e) {
   for (auto& ev : e->tev)
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
-                  e->scan_tmp, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
+                  e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
                   e->io_stage, e->stats};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -168,9 +171,10 @@ int run_pass(vgb_engine* e, int update) {
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(e->sites, e->sites_tmp, sizeof(float4) * e->n, cudaMemcpyDeviceToDevice, st));
   MARK(1);
-  if (knn_sites(e->sites, e->n, e->dim, e->cell_start, e->K, e->knn, st)) return VGB_ERR_CUDA;
+  if (knn_sites(e->sites, e->n, e->dim, e->cell_start, e->K, e->pos_of_id, e->knn, st)) return VGB_ERR_CUDA;
   MARK(2);
-  if (knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->verts, e->tets, e->n_tet, e->tk, e->cand, st))
+  if (knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
+                        e->tet_cell_start, e->n_tet, e->tk, e->cand, st))
     return VGB_ERR_CUDA;
   MARK(3);
   if (e->cfg.method == VGB_METHOD_SITE_MAJOR) {
@@ -307,7 +311,8 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if ((rc = dalloc(&e->verts, n_vert)) || (rc = dalloc(&e->tets, n_tet)) || (rc = dalloc(&e->sites, n_site)) ||
       (rc = dalloc(&e->sites_tmp, n_site)) || (rc = dalloc(&e->cell_start, e->ncell + 1)) ||
       (rc = dalloc(&e->cell_fill, e->ncell)) || (rc = dalloc(&e->site_cell, n_site)) ||
-      (rc = dalloc(&e->scan_tmp, scan_tmp_ints((long long)scan_n))) ||
+      (rc = dalloc(&e->scan_tmp, scan_tmp_ints((long long)scan_n))) || (rc = dalloc(&e->pos_of_id, n_site)) ||
+      (rc = dalloc(&e->tet_order, n_tet)) || (rc = dalloc(&e->tet_cell_start, e->ncell + 1)) ||
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method == VGB_METHOD_SITE_MAJOR ? pairs : 1)) ||
@@ -330,6 +335,19 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (ce == cudaSuccess) {
     k_pack_mesh<<<(n_vert + 255) / 256, 256, 0, e->st>>>(e->io_stage, n_vert, e->verts);
     ce = cudaMemcpyAsync(e->tets, tets, sizeof(int4) * n_tet, cudaMemcpyHostToDevice, e->st);
+  }
+  if (ce == cudaSuccess) {
+    // tets by centroid cell, once per mesh and grid
+    int* tcell = nullptr;
+    if (dalloc(&tcell, n_tet) != VGB_OK) { free_engine(e); return VGB_ERR_NOMEM; }
+    if (tets_by_cell(e->verts, e->tets, n_tet, e->dim, e->tet_cell_start, e->cell_fill, tcell, e->tet_order,
+                     e->scan_tmp, e->st)) {
+      cudaFree(tcell);
+      free_engine(e);
+      return VGB_ERR_CUDA;
+    }
+    ce = cudaStreamSynchronize(e->st);
+    cudaFree(tcell);
   }
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->stats, 0, sizeof(unsigned long long) * VGB_STAT_COUNT, e->st);
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->mom, 0, sizeof(dmom4) * n_site, e->st);

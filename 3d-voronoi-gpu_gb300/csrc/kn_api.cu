@@ -22,6 +22,7 @@ struct KnImpl {
   int* cell_fill = nullptr;
   int* site_cell = nullptr;
   int* scan_tmp = nullptr;
+  int* pos_of_id = nullptr;
 };
 
 __global__ void k_kn_pack(const float* __restrict__ xyz, int n, float4* __restrict__ out) {
@@ -53,7 +54,7 @@ void kn_release(kn_problem* kn) {
   if (!kn) return;
   KnImpl* im = static_cast<KnImpl*>(kn->impl);
   if (im) {
-    void* b[] = {im->in, im->sorted, im->cell_start, im->cell_fill, im->site_cell, im->scan_tmp};
+    void* b[] = {im->in, im->sorted, im->cell_start, im->cell_fill, im->site_cell, im->scan_tmp, im->pos_of_id};
     for (void* p : b)
       if (p) cudaFree(p);
     delete im;
@@ -98,6 +99,7 @@ int kn_prepare_ex(kn_problem** out, const float* xyz, int n, int k) {
             A((void**)&im->cell_start, sizeof(int) * (nc + 1)) && A((void**)&im->cell_fill, sizeof(int) * nc) &&
             A((void**)&im->site_cell, sizeof(int) * n) &&
             A((void**)&im->scan_tmp, sizeof(int) * scan_tmp_ints(nc + 1)) &&
+            A((void**)&im->pos_of_id, sizeof(int) * n) &&
             A((void**)&kn->d_permutation, sizeof(unsigned) * n) && A((void**)&kn->d_counters, sizeof(int) * nc) &&
             A((void**)&kn->d_ptrs, sizeof(int) * nc) && A((void**)&kn->d_globcounter, sizeof(int)) &&
             A((void**)&kn->d_stored_points, sizeof(float3) * n) &&
@@ -131,7 +133,7 @@ int kn_solve_ex(kn_problem* kn) {
   if (!kn || !kn->impl) { set_error("kn_solve: NULL problem"); return VGB_ERR_INVALID; }
   KnImpl* im = static_cast<KnImpl*>(kn->impl);
   if (knn_prepare()) return VGB_ERR_CUDA;
-  if (knn_sites(im->sorted, kn->allocated_points, kn->dimx, im->cell_start, kn->k, kn->d_knearests, 0))
+  if (knn_sites(im->sorted, kn->allocated_points, kn->dimx, im->cell_start, kn->k, im->pos_of_id, kn->d_knearests, 0))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaStreamSynchronize(0));
   return VGB_OK;

@@ -111,9 +111,19 @@ int grid_sort(const float4* in, float4* out, int n, int dim, int* cell_start, in
 
 // K nearest sorted sites of every sorted site (self excluded) or of every tet
 // centroid, ordered by (distance, id).  Output rows are sorted-space indices.
-int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, unsigned* out, cudaStream_t st);
-int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const float4* verts,
-                      const int4* tets, int n_tet, int k, unsigned* out, cudaStream_t st);
+// pos_of_id: n ints, written by knn_sites (sorted position of each id) and
+// read by knn_tet_centroids.  Centroid queries come grouped by cell:
+// tet_order / tet_cell_start from tets_by_cell.
+int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, int* pos_of_id, unsigned* out,
+              cudaStream_t st);
+int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
+                      const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
+                      int n_tet, int k, unsigned* out, cudaStream_t st);
+// Tets sorted by the grid cell of their float32 centroid (once per mesh):
+// tet_cell_start dim^3 + 1 ints, cell_fill dim^3 scratch, tcell n_tet scratch,
+// tet_order n_tet ints.
+int tets_by_cell(const float4* verts, const int4* tets, int n_tet, int dim, int* tet_cell_start, int* cell_fill,
+                 int* tcell, int* tet_order, int* scan_tmp, cudaStream_t st);
 
 // Site-major lists of candidate tets: for each site, the tets whose candidate
 // row holds it.  start: n+1 ints, fill: n ints scratch, list: n_tet*tk ints.

@@ -56,7 +56,7 @@ WORKLOADS = {
                                  desc="same torus; 1,000,000 sites from 32 Gaussians + 20% uniform; K=64"),
     # one eighth of the torus workload, for profiler captures
     "torus64_uniform_125k": dict(kind="torus", grid=64, n=125_000, sites="uniform", K=64,
-                                 desc="voxelised solid torus on a 64^3 grid (244,386 tets); 125,000 uniform sites; "
+                                 desc="voxelised solid torus on a 64^3 grid (245,088 tets); 125,000 uniform sites; "
                                       "K=64"),
     # the small configuration
     "kuhn20_20k": dict(kind="cube", cells=20, n=20000, K=64,
