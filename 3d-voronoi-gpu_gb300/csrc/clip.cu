@@ -33,9 +33,10 @@
 //     (voronoi.cu:111-116) and without dropping pieces under |vol| < 0.1
 //     (voronoi.cu:599);
 //   * each pair's volume and moment are reduced across the warp in float and
-//     accumulated per site in double registers: the per-site segmented
-//     reduction, with no global atomics (the reference adds floats
-//     atomically, voronoi.cu:605-617).
+//     accumulated per site with compensated float sums (TwoSum), written
+//     once per site in double: the per-site segmented reduction, with no
+//     global atomics (the reference adds floats atomically,
+//     voronoi.cu:605-617) and no FP64 work per pair.
 #include <cfloat>
 
 #include "vgb_common.cuh"
@@ -65,7 +66,7 @@ __device__ __forceinline__ float3 vertex_of(float4 a, float4 b, float4 c) {
   float3 ca = make_float3(c.y * a.z - c.z * a.y, c.z * a.x - c.x * a.z, c.x * a.y - c.y * a.x);
   float3 ab = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
   float det = a.x * bc.x + a.y * bc.y + a.z * bc.z;
-  float s = -1.f / det;
+  float s = __fdividef(-1.f, det);
   return make_float3(s * (a.w * bc.x + b.w * ca.x + c.w * ab.x), s * (a.w * bc.y + b.w * ca.y + c.w * ab.y),
                      s * (a.w * bc.z + b.w * ca.z + c.w * ab.z));
 }
@@ -76,6 +77,21 @@ __device__ __forceinline__ float4 face_plane(float4 p0, float4 p1, float4 p2) {
   float nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
   return make_float4(nx, ny, nz, -(nx * p0.x + ny * p0.y + nz * p0.z));
 }
+
+// Compensated float accumulator (Knuth's TwoSum): hi + lo carries the sum
+// to about twice float precision without the FP64 pipe, whose issue rate is
+// very low on GB300.
+struct CompSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float s = hi + x;
+    float bp = s - hi;
+    float e = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -98,7 +114,7 @@ __device__ __forceinline__ void vertex_moments(float3 A, float4 p0, float4 p1, f
   for (int i = 0; i < 3; ++i) {
     float4 n = pl[i];
     float nn = n.x * n.x + n.y * n.y + n.z * n.z;
-    float lam = nn > 0.f ? -n.w / nn : 0.f;
+    float lam = nn > 0.f ? __fdividef(-n.w, nn) : 0.f;
     P[2 * i] = make_float3(lam * n.x, lam * n.y, lam * n.z);
   }
 #pragma unroll
@@ -106,7 +122,7 @@ __device__ __forceinline__ void vertex_moments(float3 A, float4 p0, float4 p1, f
     float4 a = pl[i], b = pl[(i + 1) % 3];
     float dx = a.y * b.z - a.z * b.y, dy = a.z * b.x - a.x * b.z, dz = a.x * b.y - a.y * b.x;
     float dd = dx * dx + dy * dy + dz * dz;
-    float t = dd > 0.f ? (A.x * dx + A.y * dy + A.z * dz) / dd : 0.f;
+    float t = dd > 0.f ? __fdividef(A.x * dx + A.y * dy + A.z * dz, dd) : 0.f;
     P[2 * i + 1] = make_float3(A.x - t * dx, A.y - t * dy, A.z - t * dz);
   }
   v6 = 0.f;
@@ -133,10 +149,11 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
   const int wib = threadIdx.x >> 5;
   ClipWarpSmem& S = smem_all[wib];
   const unsigned lt_mask = (1u << lane) - 1u;
+  const unsigned lane_bit = 1u << lane;
 
-  unsigned long long c_cand = 0, c_culled = 0, c_clipped = 0, c_empty = 0, c_contrib = 0, c_secmiss = 0,
-                     c_overflow = 0, c_boundary = 0, c_planes = 0, c_clips = 0, c_final = 0, c_conflict = 0,
-                     c_newv = 0;
+  // per-warp counters (lane 0), flushed once per warp at the end
+  unsigned c_cand = 0, c_culled = 0, c_clipped = 0, c_empty = 0, c_contrib = 0, c_secmiss = 0, c_overflow = 0,
+           c_boundary = 0, c_planes = 0, c_clips = 0, c_final = 0, c_conflict = 0, c_newv = 0;
   unsigned c_cull_lane = 0;  // per-lane tet-vs-plane tests, summed over the warp at the end
 
   for (int s = blockIdx.x * CLIP_WARPS + wib; s < n; s += gridDim.x * CLIP_WARPS) {
@@ -149,7 +166,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
       S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
     }
     __syncwarp();
-    double V = 0.0, MX = 0.0, MY = 0.0, MZ = 0.0;
+    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
     const int cb = site_start[s], ce = site_start[s + 1];
     for (int base = cb; base < ce; base += WARP) {
       const int idx = base + lane;
@@ -227,7 +244,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
           for (int k = 0; k < TRI_SLOTS; ++k) {
             m[k] = 0u;
             if (vm[k]) {
-              bool cf = ((vm[k] >> lane) & 1u) && plane_eval(P, vx[k], vy[k], vz[k]) < 0.f;
+              bool cf = (vm[k] & lane_bit) && plane_eval(P, vx[k], vy[k], vz[k]) < 0.f;
               m[k] = __ballot_sync(FULL, cf);
               nconf += __popc(m[k]);
             }
@@ -365,7 +382,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
 #pragma unroll
         for (int k = 0; k < TRI_SLOTS; ++k)
           if ((vm[k] >> lane) & 1u) { sx += vx[k]; sy += vy[k]; sz += vz[k]; }
-        const float inv = 1.f / (float)nt;
+        const float inv = __frcp_rn((float)nt);
         const float cx = warp_sum(sx) * inv, cy = warp_sum(sy) * inv, cz = warp_sum(sz) * inv;
         float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
 #pragma unroll
@@ -392,35 +409,36 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP) k_clip_site_major(
         lmy = warp_sum(lmy);
         lmz = warp_sum(lmz);
         if (lane == 0) {
-          double vol = (double)lv / 6.0;
-          V += vol;
-          MX += (double)lmx / 24.0 + vol * (double)cx;
-          MY += (double)lmy / 24.0 + vol * (double)cy;
-          MZ += (double)lmz / 24.0 + vol * (double)cz;
+          const float vol = lv * (1.f / 6.f);
+          V.add(vol);
+          MX.add(fmaf(lmx, 1.f / 24.f, vol * cx));
+          MY.add(fmaf(lmy, 1.f / 24.f, vol * cy));
+          MZ.add(fmaf(lmz, 1.f / 24.f, vol * cz));
           c_contrib++;
         }
         __syncwarp();
       }
     }
-    if (lane == 0) mom[s] = make_dmom4(V, MX, MY, MZ);
+    if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
     __syncwarp();
   }
   const unsigned cull_warp = __reduce_add_sync(FULL, c_cull_lane);
   if (lane == 0 && stats) {
-    atomicAdd(stats + STAT_CONFLICT_TESTS, c_conflict);
-    atomicAdd(stats + STAT_CULL_TESTS, (unsigned long long)cull_warp);
-    atomicAdd(stats + STAT_NEW_VERTICES, c_newv);
-    atomicAdd(stats + STAT_CANDIDATES, c_cand);
-    atomicAdd(stats + STAT_CULLED, c_culled);
-    atomicAdd(stats + STAT_CLIPPED, c_clipped);
-    atomicAdd(stats + STAT_EMPTY, c_empty);
-    atomicAdd(stats + STAT_CONTRIB, c_contrib);
-    atomicAdd(stats + STAT_SECURITY_MISS, c_secmiss);
-    atomicAdd(stats + STAT_TRI_OVERFLOW, c_overflow);
-    atomicAdd(stats + STAT_BOUNDARY_FAIL, c_boundary);
-    atomicAdd(stats + STAT_PLANES, c_planes);
-    atomicAdd(stats + STAT_CLIPS, c_clips);
-    atomicAdd(stats + STAT_FINAL_VERTICES, c_final);
+    typedef unsigned long long u64;
+    atomicAdd(stats + STAT_CONFLICT_TESTS, (u64)c_conflict);
+    atomicAdd(stats + STAT_CULL_TESTS, (u64)cull_warp);
+    atomicAdd(stats + STAT_NEW_VERTICES, (u64)c_newv);
+    atomicAdd(stats + STAT_CANDIDATES, (u64)c_cand);
+    atomicAdd(stats + STAT_CULLED, (u64)c_culled);
+    atomicAdd(stats + STAT_CLIPPED, (u64)c_clipped);
+    atomicAdd(stats + STAT_EMPTY, (u64)c_empty);
+    atomicAdd(stats + STAT_CONTRIB, (u64)c_contrib);
+    atomicAdd(stats + STAT_SECURITY_MISS, (u64)c_secmiss);
+    atomicAdd(stats + STAT_TRI_OVERFLOW, (u64)c_overflow);
+    atomicAdd(stats + STAT_BOUNDARY_FAIL, (u64)c_boundary);
+    atomicAdd(stats + STAT_PLANES, (u64)c_planes);
+    atomicAdd(stats + STAT_CLIPS, (u64)c_clips);
+    atomicAdd(stats + STAT_FINAL_VERTICES, (u64)c_final);
   }
 }
 

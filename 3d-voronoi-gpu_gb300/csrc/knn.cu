@@ -35,7 +35,7 @@ namespace vgb {
 constexpr int KNN_THREADS = 64;
 constexpr int SEG_W = 2;             // cells per segment along x
 constexpr int STAGE_R = 2;           // staged rings around the segment
-constexpr int STAGE_CAP = 3072;      // staged sites per CTA (48 KB)
+constexpr int STAGE_CAP = 0;         // staged sites per CTA (0: rings are walked from global memory)
 constexpr int STAGE_ROWS = (2 * STAGE_R + 1) * (2 * STAGE_R + 1);
 constexpr int STAGE_ROW_CELLS = SEG_W + 2 * STAGE_R;
 constexpr float KNN_MARGIN = 0.01f;  // in [0,1000] units; cell-assignment rounding is ~1e-4
