@@ -33,7 +33,7 @@ STAT_NAMES = ["candidates", "culled", "clipped", "empty", "contrib", "security_m
               "new_vertices"]
 PHASE_NAMES = ["grid", "knn", "candidates", "site_lists", "clip", "update"]
 BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6}
-METHODS = {"site_major": 0, "plain": 1}
+METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}
 STAT_COUNT = 16
 
 
@@ -158,7 +158,7 @@ class Engine:
     """
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
-                 method: str = "site_major", use_graph: bool = True, device: int = 0):
+                 method: str = "cell_tet", use_graph: bool = True, device: int = 0):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)

@@ -1,0 +1,307 @@
+// Warp-cooperative convex cell, shared by the site-major clip kernels.
+//
+// A convex cell is kept as its dual triangulation, as in the reference
+// (voronoi.h:20-76): planes n.x + w >= 0 (inside), and triangles = three
+// plane ids = one vertex of the cell.  Here the triangles are spread over the
+// 32 lanes of a warp, TRI_SLOTS slots per lane; slot (k, lane) is live when
+// bit `lane` of vm[k] is set (vm is the same in every lane).  Each live slot
+// caches its vertex (x, y, z) and |x|^2 in registers, so testing a plane is
+// one 3-FMA evaluation per vertex and a ballot.  Plane equations live in
+// shared memory, indexed by the 8-bit plane ids.  All coordinates are
+// relative to the cell's site.
+#pragma once
+
+#include "vgb_common.cuh"
+
+namespace vgb {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+enum ClipResult : int { CLIP_NONE = 0, CLIP_CUT = 1, CLIP_EMPTY = 2, CLIP_OVERFLOW = 3, CLIP_BOUNDARY = 4 };
+
+struct WarpCell {
+  unsigned tri[TRI_SLOTS];
+  float vx[TRI_SLOTS], vy[TRI_SLOTS], vz[TRI_SLOTS], vw[TRI_SLOTS];
+  unsigned vm[TRI_SLOTS];
+  int nt;    // live triangles (warp-uniform)
+  float r2;  // max |vertex|^2 over live triangles (warp-uniform)
+};
+
+__device__ __forceinline__ unsigned pack_tri(unsigned a, unsigned b, unsigned c) { return a | (b << 8) | (c << 16); }
+__device__ __forceinline__ unsigned tri_at(unsigned t, int e) { return (t >> (8 * e)) & 0xffu; }
+
+__device__ __forceinline__ float plane_eval(float4 P, float x, float y, float z) {
+  return fmaf(P.x, x, fmaf(P.y, y, fmaf(P.z, z, P.w)));
+}
+
+// Vertex of three planes n_i.x + w_i = 0 (Cramer's rule, as a cross-product
+// combination).
+__device__ __forceinline__ float3 vertex_of(float4 a, float4 b, float4 c) {
+  float3 bc = make_float3(b.y * c.z - b.z * c.y, b.z * c.x - b.x * c.z, b.x * c.y - b.y * c.x);
+  float3 ca = make_float3(c.y * a.z - c.z * a.y, c.z * a.x - c.x * a.z, c.x * a.y - c.y * a.x);
+  float3 ab = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+  float det = a.x * bc.x + a.y * bc.y + a.z * bc.z;
+  float s = __fdividef(-1.f, det);
+  return make_float3(s * (a.w * bc.x + b.w * ca.x + c.w * ab.x), s * (a.w * bc.y + b.w * ca.y + c.w * ab.y),
+                     s * (a.w * bc.z + b.w * ca.z + c.w * ab.z));
+}
+
+// Plane through three points, normal (p1-p0)x(p2-p0): positive inside a
+// positively oriented tet for the faces (c,b,d), (a,c,d), (b,a,d), (a,b,c)
+// (voronoi.cu:119-123, 179).
+__device__ __forceinline__ float4 face_plane(float3 p0, float3 p1, float3 p2) {
+  float ux = p1.x - p0.x, uy = p1.y - p0.y, uz = p1.z - p0.z;
+  float vx = p2.x - p0.x, vy = p2.y - p0.y, vz = p2.z - p0.z;
+  float nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+  return make_float4(nx, ny, nz, -(nx * p0.x + ny * p0.y + nz * p0.z));
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
+
+// Compensated float accumulator (Knuth's TwoSum): hi + lo carries a sum to
+// about twice float precision without the FP64 pipe, whose issue rate is very
+// low on GB300.
+struct CompSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float s = hi + x;
+    float bp = s - hi;
+    float e = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ void cell_clear(WarpCell& c) {
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k) {
+    c.tri[k] = 0u;
+    c.vx[k] = c.vy[k] = c.vz[k] = c.vw[k] = 0.f;
+    c.vm[k] = 0u;
+  }
+  c.nt = 0;
+  c.r2 = 0.f;
+}
+
+// Clip the cell by plane P (id pidx): remove the vertices strictly outside,
+// then close the cavity with the fan (pidx, a, b) over its boundary edges
+// (a -> b).  The reference finds the boundary by walking the removed
+// triangles (voronoi.cu:391-441, 443-486); here a directed edge of a removed
+// triangle is on the boundary exactly when no other removed triangle holds
+// its twin, which one lane per edge decides with __match_any_sync on the
+// undirected edge key (a shared-memory search handles cavities of more than
+// ten triangles).  Each boundary vertex must start and end exactly one
+// boundary edge, else the cell is dropped (the reference's
+// inconsistent_boundary).  New triangles fill freed slots; the receiving lane
+// computes the new vertex.  conf and bedge are MAX_TRI-entry scratch arrays of
+// the warp.
+__device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsigned pidx, const float4* planes,
+                                         unsigned* conf, unsigned* bedge, const int lane) {
+  const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
+  unsigned m[TRI_SLOTS];
+  int nconf = 0;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k) {
+    m[k] = 0u;
+    if (c.vm[k]) {
+      bool cf = (c.vm[k] & lane_bit) && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
+      m[k] = __ballot_sync(FULL, cf);
+      nconf += __popc(m[k]);
+    }
+  }
+  if (nconf == 0) return CLIP_NONE;
+  if (nconf == c.nt) return CLIP_EMPTY;
+  {
+    int off = 0;
+#pragma unroll
+    for (int k = 0; k < TRI_SLOTS; ++k) {
+      if (m[k] & lane_bit) conf[off + __popc(m[k] & lt_mask)] = c.tri[k];
+      off += __popc(m[k]);
+    }
+  }
+  __syncwarp();
+  const int R = nconf;
+  int nb = 0;
+  bool bad = false;
+  if (3 * R <= WARP) {
+    const bool live = lane < 3 * R;
+    unsigned ea = 0, eb = 0;
+    if (live) {
+      unsigned T = conf[lane / 3];
+      int es = lane % 3;
+      ea = tri_at(T, es);
+      eb = tri_at(T, es == 2 ? 0 : es + 1);
+    }
+    // every lane takes part in each match (full-warp collectives)
+    const unsigned key = live ? (min(ea, eb) | (max(ea, eb) << 8)) : (0x10000u | lane);
+    const unsigned same = __match_any_sync(FULL, key);
+    const bool isb = live && __popc(same) == 1;
+    const unsigned bm = __ballot_sync(FULL, isb);
+    nb = __popc(bm);
+    const unsigned ka = isb ? ea : (0x20000u | lane), kb = isb ? eb : (0x30000u | lane);
+    const unsigned ga = __match_any_sync(FULL, ka);
+    const unsigned gb = __match_any_sync(FULL, kb);
+    bad = __any_sync(FULL, isb && (__popc(ga) != 1 || __popc(gb) != 1));
+    if (isb) bedge[__popc(bm & lt_mask)] = ea | (eb << 8);
+  } else {
+    for (int e0 = 0; e0 < 3 * R; e0 += WARP) {
+      const int e = e0 + lane;
+      bool isb = false;
+      unsigned ea = 0, eb = 0;
+      if (e < 3 * R) {
+        unsigned T = conf[e / 3];
+        int es = e % 3;
+        ea = tri_at(T, es);
+        eb = tri_at(T, es == 2 ? 0 : es + 1);
+        bool twin = false;
+        for (int q = 0; q < R; ++q) {
+          unsigned U = conf[q];
+          unsigned u0 = tri_at(U, 0), u1 = tri_at(U, 1), u2 = tri_at(U, 2);
+          twin |= (u0 == eb && u1 == ea) || (u1 == eb && u2 == ea) || (u2 == eb && u0 == ea);
+        }
+        isb = !twin;
+      }
+      unsigned bm = __ballot_sync(FULL, isb);
+      if (isb) {
+        int r = nb + __popc(bm & lt_mask);
+        if (r < MAX_TRI) bedge[r] = ea | (eb << 8);
+      }
+      nb += __popc(bm);
+    }
+    __syncwarp();
+    if (nb <= MAX_TRI) {
+      for (int e = lane; e < nb; e += WARP) {
+        unsigned E = bedge[e];
+        int starts = 0, ends = 0;
+        for (int q = 0; q < nb; ++q) {
+          unsigned F = bedge[q];
+          starts += (F & 0xffu) == (E & 0xffu);
+          ends += (F >> 8) == (E >> 8);
+        }
+        if (starts != 1 || ends != 1) bad = true;
+      }
+    }
+    bad = __any_sync(FULL, bad);
+  }
+  const int nt2 = c.nt - R + nb;
+  if (nt2 > MAX_TRI) return CLIP_OVERFLOW;
+  if (bad || nb < 3) return CLIP_BOUNDARY;
+  __syncwarp();
+  float lm = 0.f;
+  int base = 0;
+  bool nonfinite = false;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k) {
+    const unsigned keep = c.vm[k] & ~m[k];
+    const unsigned freem = ~keep;
+    const int r = base + __popc(freem & lt_mask);
+    const bool recv = (freem & lane_bit) && r < nb;
+    if (recv) {
+      unsigned E = bedge[r];
+      unsigned ea = E & 0xffu, eb = E >> 8;
+      float3 x = vertex_of(P, planes[ea], planes[eb]);
+      c.tri[k] = pack_tri(pidx, ea, eb);
+      c.vx[k] = x.x;
+      c.vy[k] = x.y;
+      c.vz[k] = x.z;
+      c.vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
+      nonfinite |= !isfinite(c.vw[k]);
+    }
+    c.vm[k] = keep | __ballot_sync(FULL, recv);
+    base += __popc(freem);
+    if (c.vm[k] & lane_bit) lm = fmaxf(lm, c.vw[k]);
+  }
+  // a new vertex from (nearly) parallel planes: the conflict decisions were
+  // inconsistent (a plane through an edge, within rounding); drop the cell
+  if (__any_sync(FULL, nonfinite)) return CLIP_BOUNDARY;
+  c.nt = nt2;
+  c.r2 = warp_max(lm);
+  __syncwarp();
+  return CLIP_CUT;
+}
+
+// Signed volume (x6) and first moment (x24) of the six sub-tets of one cell
+// vertex A, relative to an apex at the origin: feet of the apex on the
+// vertex's three faces and on its three edges (voronoi.cu:532-537, 589-597).
+// The edge foot uses the edge direction n_p x n_q: the reference's
+// projection without its n_2 > 1e-2 guard (voronoi.cu:111-116).
+__device__ __forceinline__ void vertex_moments(float3 A, float4 p0, float4 p1, float4 p2, float& v6, float3& m24) {
+  float4 pl[3] = {p0, p1, p2};
+  float3 P[6];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float4 n = pl[i];
+    float nn = n.x * n.x + n.y * n.y + n.z * n.z;
+    float lam = nn > 0.f ? __fdividef(-n.w, nn) : 0.f;
+    P[2 * i] = make_float3(lam * n.x, lam * n.y, lam * n.z);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float4 a = pl[i], b = pl[(i + 1) % 3];
+    float dx = a.y * b.z - a.z * b.y, dy = a.z * b.x - a.x * b.z, dz = a.x * b.y - a.y * b.x;
+    float dd = dx * dx + dy * dy + dz * dz;
+    float t = dd > 0.f ? __fdividef(A.x * dx + A.y * dy + A.z * dz, dd) : 0.f;
+    P[2 * i + 1] = make_float3(A.x - t * dx, A.y - t * dy, A.z - t * dz);
+  }
+  v6 = 0.f;
+  m24 = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    float3 a = P[m], b = P[(m + 1) % 6];
+    float cx = a.y * b.z - a.z * b.y, cy = a.z * b.x - a.x * b.z, cz = a.x * b.y - a.y * b.x;
+    float d = A.x * cx + A.y * cy + A.z * cz;  // det3(a, b, A)
+    v6 += d;
+    m24.x += d * (a.x + b.x + A.x);
+    m24.y += d * (a.y + b.y + A.y);
+    m24.z += d * (a.z + b.z + A.z);
+  }
+}
+
+// Volume and first moment (relative to the site) of the cell, reduced over
+// the warp.  The decomposition is taken from the mean of the cell's vertices
+// (any apex gives the same sums; an inside apex avoids cancellation), and
+// the reference's |vol| < 0.1 cut (voronoi.cu:599) is not applied.
+__device__ __forceinline__ void warp_moments(const WarpCell& c, const float4* planes, const int lane, float& vol,
+                                             float& mx, float& my, float& mz) {
+  const unsigned lane_bit = 1u << lane;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k)
+    if (c.vm[k] & lane_bit) { sx += c.vx[k]; sy += c.vy[k]; sz += c.vz[k]; }
+  const float inv = __frcp_rn((float)c.nt);
+  const float cx = warp_sum(sx) * inv, cy = warp_sum(sy) * inv, cz = warp_sum(sz) * inv;
+  float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k) {
+    if (c.vm[k] & lane_bit) {
+      const unsigned T = c.tri[k];
+      float4 q0 = planes[tri_at(T, 0)], q1 = planes[tri_at(T, 1)], q2 = planes[tri_at(T, 2)];
+      q0.w += q0.x * cx + q0.y * cy + q0.z * cz;  // planes relative to the apex
+      q1.w += q1.x * cx + q1.y * cy + q1.z * cz;
+      q2.w += q2.x * cx + q2.y * cy + q2.z * cz;
+      float v6;
+      float3 m24;
+      vertex_moments(make_float3(c.vx[k] - cx, c.vy[k] - cy, c.vz[k] - cz), q0, q1, q2, v6, m24);
+      lv += v6;
+      lmx += m24.x;
+      lmy += m24.y;
+      lmz += m24.z;
+    }
+  }
+  vol = warp_sum(lv) * (1.f / 6.f);
+  mx = fmaf(warp_sum(lmx), 1.f / 24.f, vol * cx);
+  my = fmaf(warp_sum(lmy), 1.f / 24.f, vol * cy);
+  mz = fmaf(warp_sum(lmz), 1.f / 24.f, vol * cz);
+}
+
+}  // namespace vgb

@@ -177,7 +177,7 @@ int run_pass(vgb_engine* e, int update) {
                         e->tet_cell_start, e->n_tet, e->tk, e->cand, st))
     return VGB_ERR_CUDA;
   MARK(3);
-  if (e->cfg.method == VGB_METHOD_SITE_MAJOR) {
+  if (e->cfg.method != VGB_METHOD_PLAIN) {
     if (candidates_by_site(e->cand, e->n_tet, e->tk, e->n, e->site_start, e->site_fill, e->site_tets,
                            e->scan_tmp, st))
       return VGB_ERR_CUDA;
@@ -185,9 +185,9 @@ int run_pass(vgb_engine* e, int update) {
   VGB_CUDA_TRY(cudaMemsetAsync(e->stats, 0, sizeof(unsigned long long) * VGB_STAT_COUNT, st));
   if (e->cfg.method == VGB_METHOD_PLAIN) VGB_CUDA_TRY(cudaMemsetAsync(e->mom_f, 0, sizeof(float4) * e->n, st));
   MARK(4);
-  if (e->cfg.method == VGB_METHOD_SITE_MAJOR) {
-    if (clip_tet_cell(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->site_start, e->site_tets, e->mom,
-                      e->stats, st))
+  if (e->cfg.method != VGB_METHOD_PLAIN) {
+    if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
+                        e->site_start, e->site_tets, e->mom, e->stats, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -195,7 +195,7 @@ int run_pass(vgb_engine* e, int update) {
       return VGB_ERR_CUDA;
   }
   MARK(5);
-  if (e->cfg.method == VGB_METHOD_SITE_MAJOR)
+  if (e->cfg.method != VGB_METHOD_PLAIN)
     k_finish<<<(e->n + 255) / 256, 256, 0, st>>>(e->sites, e->n, e->mom, update);
   else
     k_finish_plain<<<(e->n + 255) / 256, 256, 0, st>>>(e->sites, e->n, e->mom_f, e->mom, update);
@@ -241,7 +241,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->site_k = 90;
   cfg->tet_k = 0;
   cfg->grid_dim = 0;
-  cfg->method = VGB_METHOD_SITE_MAJOR;
+  cfg->method = VGB_METHOD_CELL_TET;
   cfg->use_graph = 1;
   cfg->device = 0;
 }
@@ -285,7 +285,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (cfg.site_k <= 0 || cfg.site_k > MAX_SITE_K || cfg.site_k >= n_site) {
     set_error("site_k=%d must be in [1, min(%d, n_site-1)]", cfg.site_k, MAX_SITE_K); return VGB_ERR_INVALID;
   }
-  if (cfg.method != VGB_METHOD_SITE_MAJOR && cfg.method != VGB_METHOD_PLAIN) {
+  if (cfg.method != VGB_METHOD_SITE_MAJOR && cfg.method != VGB_METHOD_PLAIN && cfg.method != VGB_METHOD_CELL_TET) {
     set_error("unknown method %d", cfg.method); return VGB_ERR_INVALID;
   }
   for (long long i = 0; i < 4LL * n_tet; ++i)
@@ -315,7 +315,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->tet_order, n_tet)) || (rc = dalloc(&e->tet_cell_start, e->ncell + 1)) ||
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
-      (rc = dalloc(&e->site_tets, cfg.method == VGB_METHOD_SITE_MAJOR ? pairs : 1)) ||
+      (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN ? pairs : 1)) ||
       (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
@@ -420,7 +420,7 @@ size_t vgb_engine_buffer_bytes(vgb_engine* e, int which) {
     case VGB_BUF_CAND: return sizeof(unsigned) * (size_t)e->n_tet * e->tk;
     case VGB_BUF_CELL_START: return sizeof(int) * (size_t)(e->ncell + 1);
     case VGB_BUF_SITE_START: return sizeof(int) * ((size_t)e->n + 1);
-    case VGB_BUF_SITE_TETS: return e->cfg.method == VGB_METHOD_SITE_MAJOR ? sizeof(int) * (size_t)e->n_tet * e->tk : 0;
+    case VGB_BUF_SITE_TETS: return e->cfg.method != VGB_METHOD_PLAIN ? sizeof(int) * (size_t)e->n_tet * e->tk : 0;
     case VGB_BUF_MOMENTS: return sizeof(dmom4) * e->n;
   }
   return 0;

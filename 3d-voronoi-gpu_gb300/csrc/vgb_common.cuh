@@ -130,11 +130,12 @@ int tets_by_cell(const float4* verts, const int4* tets, int n_tet, int dim, int*
 int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* start, int* fill, int* list,
                        int* scan_tmp, cudaStream_t st);
 
-// Tet-cell clipping of every candidate pair, site-major, per-site moments in
-// double relative to the site: mom[s] = (vol, mx, my, mz).
-int clip_tet_cell(const float4* sites, int n, const unsigned* knn, int k, const float4* verts, const int4* tets,
-                  const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
-                  cudaStream_t st);
+// Site-major clipping of every candidate pair -- the tet-cell method, or the
+// cell-tet method when cell_tet -- with per-site moments relative to the
+// site: mom[s] = (vol, mx, my, mz).
+int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
+                    const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
+                    unsigned long long* stats, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
 // atomics into per-site sums (the plain form).  mom_f: n float4 (vol, m).

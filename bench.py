@@ -63,7 +63,7 @@ WORKLOADS = {
                        desc="unit cube, 20^3 Kuhn grid (48,000 tets); 20,000 uniform sites; K=64"),
 }
 DEFAULT_WORKLOAD = "torus128_uniform_1m"
-LAUNCHES_PER_STEP = {"site_major": 15, "plain": 10}
+LAUNCHES_PER_STEP = {"cell_tet": 16, "site_major": 16, "plain": 11}
 
 # algorithmic FP32 work of the clip kernel, per counted event
 FLOPS_CONFLICT = 7      # plane test of one cell vertex: 3 FMA + compare
@@ -328,8 +328,10 @@ def run_ours(args):
     clip_flops = (FLOPS_CONFLICT * stats["conflict_tests"] + FLOPS_CULL * stats["cull_tests"] +
                   FLOPS_NEW_VERTEX * stats["new_vertices"] + FLOPS_FINAL_VERTEX * stats["final_vertices"])
     clip_tf = clip_flops / (phases["clip"] / 1e3) / 1e12
-    ktraffic = profile_traffic("clip_site_major" if args.method == "site_major" else "clip_plain", args.workload)
-    roofline = {"kernel": "k_clip_site_major" if args.method == "site_major" else "k_clip_plain",
+    kname = {"cell_tet": "k_clip_site<true>", "site_major": "k_clip_site<false>", "plain": "k_clip_plain"}[args.method]
+    ktraffic = profile_traffic({"cell_tet": "clip_cell_tet", "site_major": "clip_tet_cell",
+                                "plain": "clip_plain"}[args.method], args.workload)
+    roofline = {"kernel": kname,
                 "bound": "fp32", "achieved": round(clip_tf, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
                 "frac": round(clip_tf / fp32_peak, 4), "traffic": ktraffic,
                 "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock from MEASURED_PEAKS.json); "
@@ -365,7 +367,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "n_site": eng.n_site, "n_tet": eng.n_tet,
                    "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
-                   "moments": "f64 per site" if args.method == "site_major" else "f32 atomics",
+                   "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
                    "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": LAUNCHES_PER_STEP[args.method] * args.steps,
@@ -453,7 +455,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
-    ap.add_argument("--method", choices=["site_major", "plain"], default="site_major")
+    ap.add_argument("--method", choices=["cell_tet", "site_major", "plain"], default="cell_tet")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -63,8 +63,10 @@ enum vgb_stat {
 };
 
 /* Clip kernels. */
-#define VGB_METHOD_SITE_MAJOR 0 /* warp per site, FP64 per-site moments (default) */
-#define VGB_METHOD_PLAIN 1      /* thread per (tet, site) pair, float atomics      */
+#define VGB_METHOD_SITE_MAJOR 0 /* tet-cell method, warp per site, compensated per-site sums     */
+#define VGB_METHOD_PLAIN 1      /* tet-cell method, thread per (tet, site) pair, float atomics */
+#define VGB_METHOD_CELL_TET 2   /* cell-tet method, warp per site: the site's cell is built once
+                                   and clipped by each candidate tet's faces (default)         */
 
 /* Buffers readable with vgb_engine_copy_buffer. */
 enum vgb_buffer {
@@ -88,7 +90,7 @@ typedef struct vgb_config {
 
 typedef struct vgb_engine vgb_engine;
 
-/* Defaults: site_k 90, tet_k 0, grid_dim 0, site-major, graphs on, device 0. */
+/* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0. */
 void vgb_config_init(vgb_config* cfg);
 
 /* One-line description of a CUDA device (name, SMs, memory) into buf. */

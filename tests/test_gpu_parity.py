@@ -22,7 +22,7 @@ def built(pkg):
     return pkg
 
 
-def run_pass(pkg, P, K, tk=0, method="site_major", use_graph=True):
+def run_pass(pkg, P, K, tk=0, method="cell_tet", use_graph=True):
     with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, tet_k=tk, method=method, use_graph=use_graph) as e:
         e.iterate(1, update=False)
         e.sync()
@@ -40,6 +40,7 @@ def check_moments(oracle, P, g, ref):
     rv, rm = ref["vol"], ref["mom"]
     big = rv > 1e-9 * rv.max()
     rel = np.abs(vol[big] - rv[big]) / rv[big]
+    assert np.isfinite(vol).all() and np.isfinite(mom).all()
     assert rel.max() < VOL_RTOL, (rel.max(), np.argmax(rel))
     assert np.all(vol[~big] < 1e-6 * rv.max())
     b, rb = mom[big] / vol[big, None], rm[big] / rv[big, None]
@@ -55,10 +56,11 @@ def oracle_pass(oracle, g, P, K):
     return oracle.iteration(P.sites, P.verts, P.tets, K, g["tk"])
 
 
-def test_small_cube_all_stages(built, meshgen, oracle):
+@pytest.mark.parametrize("method", ["cell_tet", "site_major"])
+def test_small_cube_all_stages(built, meshgen, oracle, method):
     pkg = built
     P = meshgen.cube_problem(8, 1500, seed=7)
-    g = run_pass(pkg, P, 64)
+    g = run_pass(pkg, P, 64, method=method)
     r = oracle_pass(oracle, g, P, 64)
     assert g["dim"] == r["dim"]
     assert np.array_equal(g["ids"], r["ids"])            # grid order by (cell, id)
@@ -83,10 +85,11 @@ def test_small_cube_matches_reference_index_sets(built, meshgen):
     assert np.array_equal(ids[g["cand"]], gd["cand"])
 
 
-def test_cfg1_cube_all_stages(built, meshgen, oracle):
+@pytest.mark.parametrize("method", ["cell_tet", "site_major"])
+def test_cfg1_cube_all_stages(built, meshgen, oracle, method):
     pkg = built
     P = meshgen.cube_problem(20, 20000, seed=1)
-    g = run_pass(pkg, P, 64)
+    g = run_pass(pkg, P, 64, method=method)
     r = oracle_pass(oracle, g, P, 64)
     assert g["tk"] == 50 and g["dim"] == 19
     assert np.array_equal(g["ids"], r["ids"])
