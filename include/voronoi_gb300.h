@@ -177,6 +177,25 @@ int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const int* indic
                              int n_site, int site_is_transposed, int nb_Lloyd_iter, int preferred_tet_k,
                              int site_k, int write_files);
 
+/* Grid kNN that allocates nothing.  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc (a framework that owns the
+ * device memory pool, or a loop that cannot afford cudaMalloc's implicit
+ * device synchronisation).  Same results as kn_prepare_k + kn_solve:
+ * d_knn (n x k) holds the k nearest points of each point in grid order, as
+ * grid positions, and d_perm (n) maps grid position -> input index.  All
+ * pointers are device memory owned by the caller; d_points is n x 3 floats.
+ * Intermediate arrays live in one static device array of about 2.8 MB, held
+ * by every GPU that loads the library until the process exits, so n is at
+ * most VGB_NOALLOC_MAX_POINTS (larger n returns VGB_ERR_INVALID) and
+ * 1 <= k <= 128, k < n.  Work is queued on `stream` (a cudaStream_t, NULL for
+ * the default stream); the call returns without waiting.  The first call on
+ * a device sets up that device (cudaGetSymbolAddress, kernel attributes):
+ * make it before any stream capture.  Every call shares the static array, so
+ * calls that overlap on the GPU (other streams, other host threads) race:
+ * order them on one stream. */
+#define VGB_NOALLOC_MAX_POINTS 65536
+int vgb_knn_noalloc(const float* d_points, int n, int k, unsigned* d_knn, unsigned* d_perm, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
