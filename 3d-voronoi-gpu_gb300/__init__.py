@@ -30,7 +30,7 @@ STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
 STAT_NAMES = ["candidates", "culled", "clipped", "empty", "contrib", "security_miss", "tri_overflow",
               "boundary_fail", "planes", "clips", "final_vertices", "conflict_tests", "cull_tests",
-              "new_vertices"]
+              "new_vertices", "interior"]
 PHASE_NAMES = ["grid", "knn", "candidates", "site_lists", "clip", "update"]
 BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6}
 METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}
@@ -52,7 +52,7 @@ def build(force: bool = False) -> Path:
 
 class _Config(C.Structure):
     _fields_ = [("site_k", C.c_int), ("tet_k", C.c_int), ("grid_dim", C.c_int), ("method", C.c_int),
-                ("use_graph", C.c_int), ("device", C.c_int)]
+                ("use_graph", C.c_int), ("device", C.c_int), ("whole_interior", C.c_int)]
 
 
 class _KnProblem(C.Structure):
@@ -158,7 +158,7 @@ class Engine:
     """
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
-                 method: str = "cell_tet", use_graph: bool = True, device: int = 0):
+                 method: str = "cell_tet", use_graph: bool = True, device: int = 0, whole_interior: bool = False):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -169,6 +169,7 @@ class Engine:
         L.vgb_config_init(C.byref(cfg))
         cfg.site_k, cfg.tet_k, cfg.grid_dim = site_k, tet_k, grid_dim
         cfg.method, cfg.use_graph, cfg.device = METHODS[method], int(use_graph), device
+        cfg.whole_interior = int(whole_interior)
         h = C.c_void_p()
         _check(L.vgb_engine_create(C.byref(h), C.byref(cfg), _p(self._verts), len(self._verts), _p(self._tets),
                                    len(self._tets), _p(s), len(s)), "vgb_engine_create")

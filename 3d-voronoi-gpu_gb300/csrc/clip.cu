@@ -54,7 +54,7 @@ constexpr int BOX_PLANES = 6;
 
 enum WarpCount : int {
   WC_CAND = 0, WC_CULLED, WC_CLIPPED, WC_EMPTY, WC_CONTRIB, WC_SECMISS, WC_OVERFLOW, WC_BOUNDARY, WC_PLANES,
-  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_N
+  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_N
 };
 
 struct SiteSmem {
@@ -98,7 +98,8 @@ template <bool CELL_TET>
 __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, int K,
     const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
-    const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats) {
+    const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
+    const unsigned char* __restrict__ field, int fdim) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -119,7 +120,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     }
     float Rc = 0.f;
     int nfaces = 0;
-    bool cell_ok = true;
+    bool cell_ok = true, interior = false;
+    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
     if (CELL_TET) {
       // The reference starts the cell from the box [-0.1, 1000.1]^3
       // (voronoi.cu:125-161).  Here it starts from a cube centred on the site
@@ -166,6 +168,30 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
       if (lane == 0) { S.mnt = c.nt; S.mr2 = c.r2; }
       Rc = sqrtf(c.r2);
+      // A cell that provably lies inside the mesh is its own clipped cell:
+      // the sum over the tets it meets of (cell ^ tet) is the cell itself.
+      // field[f] = d > 0 marks an inside cell of the field grid whose points
+      // are at least (d - 1) * h from the mesh boundary; the cell lies
+      // within Rc of its site.
+      if (field && cell_ok && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
+          seed.y <= 1000.f && seed.z >= 0.f && seed.z <= 1000.f) {
+        const int fc = grid_cell(seed.x, seed.y, seed.z, fdim);
+        const int fd = field[fc];
+        const float fh = 1000.f / (float)fdim;
+        if (fd >= 2 && (float)(fd - 1) * fh > Rc * 1.001f + 0.01f) {
+          float vol, mx, my, mz;
+          warp_moments(c, S.plane, lane, vol, mx, my, mz);
+          if (lane == 0) {
+            V.add(vol);
+            MX.add(mx);
+            MY.add(my);
+            MZ.add(mz);
+            S.cnt[WC_INTERIOR]++;
+            S.cnt[WC_FINAL] += (unsigned)c.nt;
+          }
+          interior = true;
+        }
+      }
       // the planes that bound the cell (ids present in its triangles)
       unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
 #pragma unroll
@@ -187,9 +213,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       }
     }
     __syncwarp();
-    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
     const int cb = site_start[s], ce = site_start[s + 1];
-    for (int base = cb; cell_ok && base < ce; base += WARP) {
+    for (int base = cb; cell_ok && !interior && base < ce; base += WARP) {
       const int idx = base + lane;
       const bool valid = idx < ce;
       int t = -1;
@@ -348,7 +373,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     static const int slot[WC_N] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB,
                                    STAT_SECURITY_MISS, STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES,
                                    STAT_CLIPS, STAT_FINAL_VERTICES, STAT_CONFLICT_TESTS, STAT_CULL_TESTS,
-                                   STAT_NEW_VERTICES};
+                                   STAT_NEW_VERTICES, STAT_INTERIOR};
     if (S.cnt[lane]) atomicAdd(stats + slot[lane], (unsigned long long)S.cnt[lane]);
   }
 }
@@ -368,7 +393,7 @@ int clip_prepare() {
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, cudaStream_t st) {
+                    unsigned long long* stats, const unsigned char* field, int fdim, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
   // a few waves of resident blocks; sites are dealt round-robin to warps
@@ -377,10 +402,10 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   int blocks = (int)(want < need ? want : need);
   if (cell_tet)
     k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                            mom, stats);
+                                                            mom, stats, field, fdim);
   else
     k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                             mom, stats);
+                                                             mom, stats, nullptr, 0);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <new>
 #include <vector>
 
@@ -49,6 +50,8 @@ struct vgb_engine {
   float4* mom_f = nullptr;
   float* io_stage = nullptr;  // n x 3 floats for host-buffer steps
   unsigned long long* stats = nullptr;
+  unsigned char* field = nullptr;  // inside field for whole interior cells (or null)
+  int fdim = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -154,7 +157,7 @@ void free_engine(vgb_engine* e) {
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
-                  e->io_stage, e->stats};
+                  e->io_stage, e->stats, e->field};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -187,7 +190,7 @@ int run_pass(vgb_engine* e, int update) {
   MARK(4);
   if (e->cfg.method != VGB_METHOD_PLAIN) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
-                        e->site_start, e->site_tets, e->mom, e->stats, st))
+                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->fdim, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -244,6 +247,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->method = VGB_METHOD_CELL_TET;
   cfg->use_graph = 1;
   cfg->device = 0;
+  cfg->whole_interior = 0;
 }
 
 const char* vgb_last_error(void) { return vgb::last_error(); }
@@ -353,6 +357,15 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->mom, 0, sizeof(dmom4) * n_site, e->st);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
   if (ce != cudaSuccess) { set_error("mesh upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
+  if (cfg.method == VGB_METHOD_CELL_TET && cfg.whole_interior) {
+    // field grid twice as fine as the site grid, at most 512 per side
+    e->fdim = std::min(512, std::max(8, 2 * e->dim));
+    std::vector<unsigned char> field;
+    build_inside_field(verts, n_vert, tets, n_tet, e->fdim, field);
+    if ((rc = dalloc(&e->field, field.size()))) { free_engine(e); return rc; }
+    ce = cudaMemcpy(e->field, field.data(), field.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
+  }
   if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
   *out = e;
   return VGB_OK;

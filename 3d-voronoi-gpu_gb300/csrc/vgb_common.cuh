@@ -38,6 +38,7 @@ enum StatSlot : int {
   STAT_CONFLICT_TESTS = 11,  // vertex-vs-plane tests of the clip loop
   STAT_CULL_TESTS = 12,      // tet-vs-plane tests of the separation pass
   STAT_NEW_VERTICES = 13,    // vertices created by clipping
+  STAT_INTERIOR = 14,        // sites whose whole cell lies inside the mesh (taken whole)
   STAT_COUNT = 16
 };
 
@@ -133,9 +134,11 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 // Site-major clipping of every candidate pair -- the tet-cell method, or the
 // cell-tet method when cell_tet -- with per-site moments relative to the
 // site: mom[s] = (vol, mx, my, mz).
+// field (fdim^3 bytes, from build_inside_field) enables taking cells that lie
+// inside the mesh whole (cell-tet only); nullptr disables it.
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, cudaStream_t st);
+                    unsigned long long* stats, const unsigned char* field, int fdim, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
 // atomics into per-site sums (the plain form).  mom_f: n float4 (vol, m).
@@ -148,4 +151,10 @@ int knn_prepare();
 int clip_prepare();
 
 
+}  // namespace vgb
+
+#include <vector>
+namespace vgb {
+// Inside field of a mesh on a dim^3 grid over [0,1000]^3 (mesh_field.cpp).
+int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim, std::vector<unsigned char>& field);
 }  // namespace vgb

@@ -270,7 +270,9 @@ def run_ours(args):
     w = WORKLOADS[args.workload]
     P = make_problem(args.workload)
     K = w["K"]
-    eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local)
+    whole = args.method == "cell_tet" and not args.per_tet
+    eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
+                     whole_interior=whole)
 
     def barrier():
         if dist:
@@ -367,6 +369,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "n_site": eng.n_site, "n_tet": eng.n_tet,
                    "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
+                   "interior_cells": "whole" if whole else "per tet",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
                    "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
                    "parallelism": f"replicas x{world}"},
@@ -456,6 +459,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--method", choices=["cell_tet", "site_major", "plain"], default="cell_tet")
+    ap.add_argument("--per-tet", action="store_true",
+                    help="cell-tet: sum every cell over its candidate tets, as the reference does, instead of "
+                         "taking cells that lie inside the mesh whole")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

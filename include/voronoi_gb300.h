@@ -59,6 +59,7 @@ enum vgb_stat {
   VGB_STAT_CONFLICT_TESTS = 11, /* vertex-vs-plane tests while clipping               */
   VGB_STAT_CULL_TESTS = 12,     /* tet-vs-plane tests of the separation pass          */
   VGB_STAT_NEW_VERTICES = 13,   /* vertices created by clipping                       */
+  VGB_STAT_INTERIOR = 14,       /* sites whose whole cell lies inside the mesh        */
   VGB_STAT_COUNT = 16
 };
 
@@ -86,11 +87,15 @@ typedef struct vgb_config {
   int method;   /* VGB_METHOD_*                                                          */
   int use_graph;/* capture one Lloyd iteration as a CUDA graph and replay it             */
   int device;   /* CUDA device ordinal                                                   */
+  int whole_interior; /* cell-tet: a site whose cell provably lies inside the mesh takes
+                         the cell whole instead of summing it over its candidate tets
+                         (equal when the candidate set is complete; exact otherwise)     */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;
 
-/* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0. */
+/* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0,
+ * whole_interior off (the reference's per-tet sums). */
 void vgb_config_init(vgb_config* cfg);
 
 /* One-line description of a CUDA device (name, SMs, memory) into buf. */

@@ -209,3 +209,39 @@ def test_invalid_arguments_raise(built, meshgen):
         pkg.Engine(P.verts, bad, P.sites, site_k=8)
     with pytest.raises(pkg.VoronoiError):
         pkg.Engine(P.verts, P.tets, P.sites, site_k=200)  # above the supported maximum
+
+
+def test_whole_interior_cells_match_oracle(built, meshgen, oracle):
+    """Cells that provably lie inside the mesh are taken whole.  With complete
+    candidate sets (large tet_k) the reference's per-tet sums equal the whole
+    cells, so the oracle is the bar; boundary cells still go tet by tet."""
+    pkg = built
+    P = meshgen.cube_problem(20, 20000, seed=1)
+    tk = 100
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, whole_interior=True) as e:
+        e.iterate(1, update=False)
+        e.sync()
+        s4 = e.buffer("sites")
+        g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats(), tk=e.tet_k)
+        g["vol"], g["mom"] = e.moments()
+    r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
+    assert np.array_equal(g["ids"], r["ids"])
+    assert g["stats"]["interior"] > len(P.sites) // 5
+    check_moments(oracle, P, g, r)
+
+
+def test_whole_interior_on_torus(built, meshgen, oracle):
+    """A non-convex mesh: the voxelised torus (32^3), uniform sites."""
+    pkg = built
+    P = meshgen.torus_problem(6000, grid=32, seed=4)
+    tk = 100
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, whole_interior=True) as e:
+        e.iterate(1, update=False)
+        e.sync()
+        s4 = e.buffer("sites")
+        g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
+        g["vol"], g["mom"] = e.moments()
+    r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
+    assert np.array_equal(g["ids"], r["ids"])
+    assert g["stats"]["interior"] > 0
+    check_moments(oracle, P, g, r)
