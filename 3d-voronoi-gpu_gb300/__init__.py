@@ -52,7 +52,7 @@ def build(force: bool = False) -> Path:
 
 class _Config(C.Structure):
     _fields_ = [("site_k", C.c_int), ("tet_k", C.c_int), ("grid_dim", C.c_int), ("method", C.c_int),
-                ("use_graph", C.c_int), ("device", C.c_int), ("whole_interior", C.c_int)]
+                ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int)]
 
 
 class _KnProblem(C.Structure):
@@ -154,11 +154,13 @@ class Engine:
 
     verts (nv,3) float32 and sites (n,3) float32 in [0,1000]^3, tets (nt,4)
     int32 positively oriented.  Site i of the input keeps id i; the engine
-    stores sites in grid order.
+    stores sites in grid order.  exact=True (cell-tet): cells inside the mesh
+    are taken whole and the others are clipped by every tet within reach,
+    instead of the reference's per-tet sums over tet_k candidates.
     """
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
-                 method: str = "cell_tet", use_graph: bool = True, device: int = 0, whole_interior: bool = False):
+                 method: str = "cell_tet", use_graph: bool = True, device: int = 0, exact: bool = False):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -169,7 +171,7 @@ class Engine:
         L.vgb_config_init(C.byref(cfg))
         cfg.site_k, cfg.tet_k, cfg.grid_dim = site_k, tet_k, grid_dim
         cfg.method, cfg.use_graph, cfg.device = METHODS[method], int(use_graph), device
-        cfg.whole_interior = int(whole_interior)
+        cfg.exact = int(exact)
         h = C.c_void_p()
         _check(L.vgb_engine_create(C.byref(h), C.byref(cfg), _p(self._verts), len(self._verts), _p(self._tets),
                                    len(self._tets), _p(s), len(s)), "vgb_engine_create")

@@ -99,7 +99,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, int K,
     const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
     const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
-    const unsigned char* __restrict__ field, int fdim) {
+    const unsigned char* __restrict__ field, int fdim, const int* __restrict__ tet_order,
+    const int* __restrict__ tet_cell_start, int dim, float rt_max, const float* __restrict__ reach,
+    const unsigned* __restrict__ reach_max_bits) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -213,14 +215,39 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       }
     }
     __syncwarp();
-    const int cb = site_start[s], ce = site_start[s + 1];
-    for (int base = cb; cell_ok && !interior && base < ce; base += WARP) {
+    // Candidate tets, as segments of a list: the site's candidate list (the
+    // reference's tet_k sets), or, in the exact form, the x-runs of
+    // centroid-grid cells within reach of the cell -- a tet meeting the cell
+    // has its centroid within Rc + rt_max of the site.
+    const bool exact = tet_order != nullptr;
+    int nseg = 1, nj = 1, i0 = 0, i1 = 0, j0 = 0, k0 = 0;
+    if (exact && cell_ok && !interior) {
+      // no cell reaches a tet whose centroid is farther than the largest reach
+      const float R = fminf(Rc + rt_max * 1.001f, __uint_as_float(*reach_max_bits)) + 0.01f;
+      i0 = grid_axis(seed.x - R, dim);
+      i1 = grid_axis(seed.x + R, dim);
+      j0 = grid_axis(seed.y - R, dim);
+      k0 = grid_axis(seed.z - R, dim);
+      nj = grid_axis(seed.y + R, dim) - j0 + 1;
+      nseg = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
+    }
+    for (int q = 0; cell_ok && !interior && q < nseg; ++q) {
+    int sb, se;
+    if (exact) {
+      const int row = dim * ((j0 + q % nj) + dim * (k0 + q / nj));
+      sb = tet_cell_start[i0 + row];
+      se = tet_cell_start[i1 + row + 1];
+    } else {
+      sb = site_start[s];
+      se = site_start[s + 1];
+    }
+    for (int base = sb; base < se; base += WARP) {
       const int idx = base + lane;
-      const bool valid = idx < ce;
+      const bool valid = idx < se;
       int t = -1;
       float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
       if (valid) {
-        t = site_tets[idx];
+        t = exact ? tet_order[idx] : site_tets[idx];
         int4 q = tets[t];
         float4 a = verts[q.x], b = verts[q.y], cc = verts[q.z], d = verts[q.w];
         v0 = make_float3(a.x - seed.x, a.y - seed.y, a.z - seed.z);
@@ -239,6 +266,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
         const float dm = sqrtf(mx * mx + my * my + mz * mz);
         if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
+        // exact form: the tet has a site nearer than this one everywhere
+        if (exact && valid && dm > reach[t] * 1.0001f + 1e-2f) alive = false;
         // a tet whose four corners are strictly outside one face of the cell
         // cannot meet it
         for (int f = 0; f < nfaces; ++f) {
@@ -274,7 +303,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         }
       }
       const unsigned survivors = __ballot_sync(FULL, alive);
-      const int nvalid = min(WARP, ce - base), nsurv = __popc(survivors);
+      const int nvalid = min(WARP, se - base), nsurv = __popc(survivors);
       if (alive) S.queue[__popc(survivors & lt_mask)] = (unsigned)t;
       if (lane == 0) {
         S.cnt[WC_CAND] += (unsigned)nvalid;
@@ -363,6 +392,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         __syncwarp();
       }
     }
+    }
     if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
     __syncwarp();
   }
@@ -393,7 +423,9 @@ int clip_prepare() {
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, int fdim, cudaStream_t st) {
+                    unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
+                    const int* tet_cell_start, int dim, float rt_max, const float* reach,
+                    const unsigned* reach_max_bits, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
   // a few waves of resident blocks; sites are dealt round-robin to warps
@@ -402,10 +434,12 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   int blocks = (int)(want < need ? want : need);
   if (cell_tet)
     k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                            mom, stats, field, fdim);
+                                                            mom, stats, field, fdim, tet_order, tet_cell_start, dim,
+                                                            rt_max, reach, reach_max_bits);
   else
     k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                             mom, stats, nullptr, 0);
+                                                             mom, stats, nullptr, 0, nullptr, nullptr, 0, 0.f, nullptr,
+                                                             nullptr);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

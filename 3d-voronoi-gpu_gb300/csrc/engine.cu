@@ -50,8 +50,11 @@ struct vgb_engine {
   float4* mom_f = nullptr;
   float* io_stage = nullptr;  // n x 3 floats for host-buffer steps
   unsigned long long* stats = nullptr;
-  unsigned char* field = nullptr;  // inside field for whole interior cells (or null)
+  unsigned char* field = nullptr;  // exact form: inside field of the mesh (else null)
   int fdim = 0;
+  float rt_max = 0.f;              // exact form: largest tet corner distance from its centroid
+  float* reach = nullptr;          // exact form: per-tet reach (n_tet)
+  unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -157,7 +160,7 @@ void free_engine(vgb_engine* e) {
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
-                  e->io_stage, e->stats, e->field};
+                  e->io_stage, e->stats, e->field, e->reach, e->reach_max};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -176,11 +179,16 @@ int run_pass(vgb_engine* e, int update) {
   MARK(1);
   if (knn_sites(e->sites, e->n, e->dim, e->cell_start, e->K, e->pos_of_id, e->knn, st)) return VGB_ERR_CUDA;
   MARK(2);
-  if (knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
+  const bool exact = e->field != nullptr;
+  if (exact && tet_reach(e->sites, e->dim, e->cell_start, e->verts, e->tets, e->tet_order, e->n_tet, e->reach,
+                         e->reach_max, st))
+    return VGB_ERR_CUDA;
+  if (!exact &&
+      knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
                         e->tet_cell_start, e->n_tet, e->tk, e->cand, st))
     return VGB_ERR_CUDA;
   MARK(3);
-  if (e->cfg.method != VGB_METHOD_PLAIN) {
+  if (!exact && e->cfg.method != VGB_METHOD_PLAIN) {
     if (candidates_by_site(e->cand, e->n_tet, e->tk, e->n, e->site_start, e->site_fill, e->site_tets,
                            e->scan_tmp, st))
       return VGB_ERR_CUDA;
@@ -190,7 +198,9 @@ int run_pass(vgb_engine* e, int update) {
   MARK(4);
   if (e->cfg.method != VGB_METHOD_PLAIN) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
-                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->fdim, st))
+                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->fdim,
+                        exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->dim, e->rt_max,
+                        e->reach, e->reach_max, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -247,7 +257,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->method = VGB_METHOD_CELL_TET;
   cfg->use_graph = 1;
   cfg->device = 0;
-  cfg->whole_interior = 0;
+  cfg->exact = 0;
 }
 
 const char* vgb_last_error(void) { return vgb::last_error(); }
@@ -311,15 +321,16 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (ce != cudaSuccess) { set_error("stream: %s", cudaGetErrorString(ce)); delete e; return VGB_ERR_CUDA; }
   int rc = VGB_OK;
   size_t pairs = (size_t)n_tet * e->tk;
+  const bool exact_form = cfg.method == VGB_METHOD_CELL_TET && cfg.exact;
   size_t scan_n = std::max((size_t)e->ncell + 1, (size_t)n_site + 1);
   if ((rc = dalloc(&e->verts, n_vert)) || (rc = dalloc(&e->tets, n_tet)) || (rc = dalloc(&e->sites, n_site)) ||
       (rc = dalloc(&e->sites_tmp, n_site)) || (rc = dalloc(&e->cell_start, e->ncell + 1)) ||
       (rc = dalloc(&e->cell_fill, e->ncell)) || (rc = dalloc(&e->site_cell, n_site)) ||
       (rc = dalloc(&e->scan_tmp, scan_tmp_ints((long long)scan_n))) || (rc = dalloc(&e->pos_of_id, n_site)) ||
       (rc = dalloc(&e->tet_order, n_tet)) || (rc = dalloc(&e->tet_cell_start, e->ncell + 1)) ||
-      (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, pairs)) ||
+      (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
-      (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN ? pairs : 1)) ||
+      (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
       (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
@@ -357,12 +368,30 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->mom, 0, sizeof(dmom4) * n_site, e->st);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
   if (ce != cudaSuccess) { set_error("mesh upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
-  if (cfg.method == VGB_METHOD_CELL_TET && cfg.whole_interior) {
+  if (cfg.method == VGB_METHOD_CELL_TET && cfg.exact) {
     // field grid twice as fine as the site grid, at most 512 per side
     e->fdim = std::min(512, std::max(8, 2 * e->dim));
     std::vector<unsigned char> field;
     build_inside_field(verts, n_vert, tets, n_tet, e->fdim, field);
-    if ((rc = dalloc(&e->field, field.size()))) { free_engine(e); return rc; }
+    float rt = 0.f;
+    for (int t = 0; t < n_tet; ++t) {
+      const float* p[4];
+      float c[3] = {0.f, 0.f, 0.f};
+      for (int q = 0; q < 4; ++q) {
+        p[q] = verts + 3 * (size_t)tets[4 * (size_t)t + q];
+        for (int d = 0; d < 3; ++d) c[d] += 0.25f * p[q][d];
+      }
+      for (int q = 0; q < 4; ++q) {
+        float dx = p[q][0] - c[0], dy = p[q][1] - c[1], dz = p[q][2] - c[2];
+        rt = std::max(rt, std::sqrt(dx * dx + dy * dy + dz * dz));
+      }
+    }
+    e->rt_max = rt * 1.001f + 1e-3f;
+    if ((rc = dalloc(&e->field, field.size())) || (rc = dalloc(&e->reach, n_tet)) ||
+        (rc = dalloc(&e->reach_max, 1))) {
+      free_engine(e);
+      return rc;
+    }
     ce = cudaMemcpy(e->field, field.data(), field.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   }
@@ -430,10 +459,11 @@ size_t vgb_engine_buffer_bytes(vgb_engine* e, int which) {
   switch (which) {
     case VGB_BUF_SITES: return sizeof(float4) * e->n;
     case VGB_BUF_KNN: return sizeof(unsigned) * (size_t)e->n * e->K;
-    case VGB_BUF_CAND: return sizeof(unsigned) * (size_t)e->n_tet * e->tk;
+    case VGB_BUF_CAND: return e->field ? 0 : sizeof(unsigned) * (size_t)e->n_tet * e->tk;
     case VGB_BUF_CELL_START: return sizeof(int) * (size_t)(e->ncell + 1);
     case VGB_BUF_SITE_START: return sizeof(int) * ((size_t)e->n + 1);
-    case VGB_BUF_SITE_TETS: return e->cfg.method != VGB_METHOD_PLAIN ? sizeof(int) * (size_t)e->n_tet * e->tk : 0;
+    case VGB_BUF_SITE_TETS:
+      return e->cfg.method != VGB_METHOD_PLAIN && !e->field ? sizeof(int) * (size_t)e->n_tet * e->tk : 0;
     case VGB_BUF_MOMENTS: return sizeof(dmom4) * e->n;
   }
   return 0;

@@ -334,6 +334,92 @@ int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start
 }
 
 // ---------------------------------------------------------------------------
+// Reach of each tet (exact form): reach[t] = d1 + 2 r, d1 the distance from
+// its centroid to the nearest site, r its largest corner distance from the
+// centroid.  Every point x of the tet has a site within d1 + r, so a site s
+// whose cell meets the tet satisfies |s - centroid| <= reach[t].  The largest
+// reach bounds every cell's search radius.  Thread per tet, in centroid-cell
+// order; a ring walk keeps the single nearest site.
+// ---------------------------------------------------------------------------
+__global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int* __restrict__ cell_start,
+                            const float4* __restrict__ verts, const int4* __restrict__ tets,
+                            const int* __restrict__ tet_order, int n_tet, float* __restrict__ reach,
+                            unsigned* __restrict__ reach_max_bits) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  float rr = 0.f;
+  if (q < n_tet) {
+    const int t = tet_order[q];
+    const int4 v = tets[t];
+    const float4 a = verts[v.x], b = verts[v.y], c = verts[v.z], d = verts[v.w];
+    float4 Q;
+    Q.x = 0.25f * (a.x + b.x + c.x + d.x);
+    Q.y = 0.25f * (a.y + b.y + c.y + d.y);
+    Q.z = 0.25f * (a.z + b.z + c.z + d.z);
+    Q.w = 0.f;
+    float r2 = 0.f;
+    const float4 cs[4] = {a, b, c, d};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float dx = cs[i].x - Q.x, dy = cs[i].y - Q.y, dz = cs[i].z - Q.z;
+      r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+    }
+    const float h = 1000.f / (float)dim;
+    const int ci = grid_axis(Q.x, dim), cj = grid_axis(Q.y, dim), ck = grid_axis(Q.z, dim);
+    float best = FLT_MAX;
+    for (int r = 0;; ++r) {
+      bool left = (ci - r >= 0) || (ci + r <= dim - 1) || (cj - r >= 0) || (cj + r <= dim - 1) || (ck - r >= 0) ||
+                  (ck + r <= dim - 1);
+      if (!left) break;
+      if (r > 0 && best < FLT_MAX) {
+        float L = ring_bound(Q, ci, cj, ck, r, dim, h);
+        if (L == FLT_MAX) break;
+        L -= KNN_MARGIN;
+        if (L > 0.f && best < L * L) break;
+      }
+      for (int dk = -r; dk <= r; ++dk) {
+        const int k = ck + dk;
+        if (k < 0 || k >= dim) continue;
+        for (int dj = -r; dj <= r; ++dj) {
+          const int j = cj + dj;
+          if (j < 0 || j >= dim) continue;
+          const bool face = (dk == -r || dk == r || dj == -r || dj == r);
+          for (int di = -r; di <= r; di += (face || r == 0) ? 1 : 2 * r) {
+            const int i = ci + di;
+            if (i < 0 || i >= dim) continue;
+            if (best < FLT_MAX && box_d2(Q, i, j, k, dim, h) > best) continue;
+            const int cc = i + dim * (j + dim * k);
+            for (int p = cell_start[cc]; p < cell_start[cc + 1]; ++p) best = fminf(best, dist2(Q, sites[p]));
+          }
+        }
+      }
+    }
+    rr = (sqrtf(best) + 2.f * sqrtf(r2)) * 1.0001f + 1e-3f;
+    reach[t] = rr;
+  }
+  // block max, then one atomic per block (non-negative floats order as ints)
+  __shared__ float bmax[8];
+  float m = rr;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) bmax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, bmax[w]);
+    atomicMax(reach_max_bits, __float_as_uint(m));
+  }
+}
+
+int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* verts, const int4* tets,
+              const int* tet_order, int n_tet, float* reach, unsigned* reach_max_bits, cudaStream_t st) {
+  VGB_CUDA_TRY(cudaMemsetAsync(reach_max_bits, 0, sizeof(unsigned), st));
+  if (n_tet <= 0) return 0;
+  k_tet_reach<<<(n_tet + 255) / 256, 256, 0, st>>>(sites, dim, cell_start, verts, tets, tet_order, n_tet, reach,
+                                                   reach_max_bits);
+  VGB_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Tets by centroid cell (once per mesh and grid): counting sort of the tets
 // by the cell of their float32 centroid.
 // ---------------------------------------------------------------------------

@@ -120,6 +120,11 @@ int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k,
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, cudaStream_t st);
+// Exact form: reach[t] = (distance from the centroid of t to its nearest
+// site) + 2 (largest corner distance from the centroid); *reach_max_bits =
+// float bits of the largest reach.  Sites must be grid-sorted.
+int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* verts, const int4* tets,
+              const int* tet_order, int n_tet, float* reach, unsigned* reach_max_bits, cudaStream_t st);
 // Tets sorted by the grid cell of their float32 centroid (once per mesh):
 // tet_cell_start dim^3 + 1 ints, cell_fill dim^3 scratch, tcell n_tet scratch,
 // tet_order n_tet ints.
@@ -134,11 +139,16 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 // Site-major clipping of every candidate pair -- the tet-cell method, or the
 // cell-tet method when cell_tet -- with per-site moments relative to the
 // site: mom[s] = (vol, mx, my, mz).
-// field (fdim^3 bytes, from build_inside_field) enables taking cells that lie
-// inside the mesh whole (cell-tet only); nullptr disables it.
+// Exact form (cell-tet only; all of field, tet_order and tet_cell_start
+// given): cells inside the mesh (field: fdim^3 bytes from build_inside_field)
+// are taken whole, other cells are clipped by every tet whose centroid is
+// within Rc + rt_max (tets sorted by centroid cell of the site grid, dim^3
+// cells).  Otherwise the candidate lists site_start / site_tets are used.
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, int fdim, cudaStream_t st);
+                    unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
+                    const int* tet_cell_start, int dim, float rt_max, const float* reach,
+                    const unsigned* reach_max_bits, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
 // atomics into per-site sums (the plain form).  mom_f: n float4 (vol, m).

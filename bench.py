@@ -170,13 +170,31 @@ def profile_traffic(kernel: str, workload: str):
 
 
 # ---------------------------------------------------------------------------
-def host_sample_baseline(checker, sites, knn, verts, tets, cand, target_s: float = 12.0, threads: int = 0):
+def host_sample_baseline(checker, sites, knn, verts, tets, cand, target_s: float = 12.0, threads: int = 0,
+                         tk: int = 0):
     """Reference kernels (host build) on contiguous chunks of tets; returns the
     extrapolated seconds of one Lloyd iteration's clipping work (tet-cell +
-    cell-tet, as the reference runs both every iteration) and the details."""
+    cell-tet, as the reference runs both every iteration) and the details.
+    cand: the n_tet x tk candidate array, or a function giving the rows of
+    given tets (only sampled rows are needed)."""
     import ctypes as C
     n, K = knn.shape
-    nt, tk = cand.shape
+    nt = len(tets)
+    if callable(cand):
+        rows_fn = cand
+        cand = np.zeros((nt, tk), np.int32)
+        filled = np.zeros(nt, bool)
+
+        def ensure(ts):
+            need = ts[~filled[ts]]
+            if len(need):
+                cand[need] = rows_fn(need)
+                filled[need] = True
+    else:
+        tk = cand.shape[1]
+
+        def ensure(ts):
+            pass
     threads = threads or os.cpu_count() or 1
     try:
         L = checker.ref_lib(K)
@@ -209,21 +227,24 @@ def host_sample_baseline(checker, sites, knn, verts, tets, cand, target_s: float
         L.ref_time_cells.argtypes = [vp, vp, C.c_int, C.c_int]
         L.ref_time_cells.restype = C.c_double
         P = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
-        h = L.ref_prepare(P(sites), n, P(knn), P(verts), len(verts), P(tets), nt, P(cand), tk)
 
         def run(frac):
             ts = chunks(frac)
+            ensure(ts)
+            h = L.ref_prepare(P(sites), n, P(knn), P(verts), len(verts), P(tets), nt, P(cand), tk)
             pairs = (ts[:, None] * tk + np.arange(tk)[None, :]).ravel().astype(np.int64)
             need = np.unique(cand[ts]).astype(np.int32)
             t_tc = L.ref_time_tet_cell(h, P(pairs), len(pairs), threads)
             t_cells = L.ref_time_cells(h, P(need), len(need), threads)
             t_ct = L.ref_time_cell_tet(h, P(pairs), len(pairs), threads)
+            L.ref_release(h)
             return len(pairs), len(need), t_tc, t_cells, t_ct
     else:
         threads = 1
 
         def run(frac):
             ts = chunks(frac)
+            ensure(ts)
             t0 = time.perf_counter()
             checker.tet_cell(sites, knn, verts, tets[ts], cand[ts], mode=checker.SHIPPED)
             t_tc = time.perf_counter() - t0
@@ -237,8 +258,6 @@ def host_sample_baseline(checker, sites, knn, verts, tets, cand, target_s: float
     per_pair = (t_tc + t_ct) / npair + t_cells / max(1, npair)
     frac = min(0.5, max(0.002, target_s / max(1e-9, per_pair * nt * tk) * 1.0))
     npair, nneed, t_tc, t_cells, t_ct = run(frac)
-    if kind == "reference":
-        L.ref_release(h)
     total_pairs = nt * tk
     t_iter = (t_tc + t_ct) * total_pairs / npair + t_cells * n / max(1, nneed)
     detail = dict(kind=kind, cores=threads, sample_pairs=int(npair), sample_sites=int(nneed),
@@ -270,9 +289,9 @@ def run_ours(args):
     w = WORKLOADS[args.workload]
     P = make_problem(args.workload)
     K = w["K"]
-    whole = args.method == "cell_tet" and not args.per_tet
+    exact = args.method == "cell_tet" and not args.reference_form
     eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
-                     whole_interior=whole)
+                     exact=exact)
 
     def barrier():
         if dist:
@@ -351,8 +370,16 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         checker = load_checker()
         s4 = eng.buffer("sites")
+        # the reference's kernels need its tet_k candidate sets: rows of the sampled tets from the same
+        # exact search (grid kNN of the centroids, ties by site id)
+        cent = checker.tet_centroids(P.verts, P.tets)
+        ids = s4[:, 3].copy().view(np.int32)
+
+        def cand_rows(ts):
+            return checker.knn_grid(s4[:, :3], cent[ts], eng.tet_k, exclude_self=False, key=ids)
+
         t_iter, det = host_sample_baseline(checker, s4[:, :3], eng.buffer("knn").astype(np.int32), P.verts,
-                                           P.tets, eng.buffer("cand").astype(np.int32))
+                                           P.tets, cand_rows, tk=eng.tet_k)
         cpu = {"value": 1.0 / t_iter, "unit": UNIT, "cores": det["cores"], "kind": det["kind"],
                "sample": f"{det['sample_pairs']} of {eng.n_tet * eng.tet_k} (tet, site) pairs in 8 contiguous "
                          f"tet chunks plus the Voronoi cells of their {det['sample_sites']} sites; the reference's "
@@ -369,11 +396,12 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "n_site": eng.n_site, "n_tet": eng.n_tet,
                    "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
-                   "interior_cells": "whole" if whole else "per tet",
+                   "form": "exact (inside cells whole, boundary cells against every tet in reach)" if exact
+                           else "reference (per-tet sums over tet_k candidates)",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
                    "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
                    "parallelism": f"replicas x{world}"},
-        "gpu_launches": LAUNCHES_PER_STEP[args.method] * args.steps,
+        "gpu_launches": (11 if exact else LAUNCHES_PER_STEP[args.method]) * args.steps,
         "e2e": e2e,
         "roofline": roofline,
         "roofline_knn": roofline_knn,
@@ -459,9 +487,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--method", choices=["cell_tet", "site_major", "plain"], default="cell_tet")
-    ap.add_argument("--per-tet", action="store_true",
-                    help="cell-tet: sum every cell over its candidate tets, as the reference does, instead of "
-                         "taking cells that lie inside the mesh whole")
+    ap.add_argument("--reference-form", action="store_true",
+                    help="cell-tet: sum every cell over its tet_k candidate tets, as the reference does, instead "
+                         "of the exact form (cells inside the mesh whole, the rest against every tet in reach)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -73,7 +73,7 @@ enum vgb_stat {
 enum vgb_buffer {
   VGB_BUF_SITES = 0,      /* float4[n]: x, y, z, original id (int bits), grid order */
   VGB_BUF_KNN = 1,        /* uint32[n][site_k]: neighbours in grid order           */
-  VGB_BUF_CAND = 2,       /* uint32[n_tet][tet_k]: candidate sites per tet          */
+  VGB_BUF_CAND = 2,       /* uint32[n_tet][tet_k]: candidate sites per tet (not in the exact form) */
   VGB_BUF_CELL_START = 3, /* int32[grid_dim^3 + 1]                                  */
   VGB_BUF_SITE_START = 4, /* int32[n + 1]: start of each site's candidate tets      */
   VGB_BUF_SITE_TETS = 5,  /* int32[n_tet * tet_k]                                   */
@@ -87,15 +87,17 @@ typedef struct vgb_config {
   int method;   /* VGB_METHOD_*                                                          */
   int use_graph;/* capture one Lloyd iteration as a CUDA graph and replay it             */
   int device;   /* CUDA device ordinal                                                   */
-  int whole_interior; /* cell-tet: a site whose cell provably lies inside the mesh takes
-                         the cell whole instead of summing it over its candidate tets
-                         (equal when the candidate set is complete; exact otherwise)     */
+  int exact;    /* cell-tet only.  0: the reference's form -- every cell summed over the
+                   tets of its tet_k candidate sets.  1: the exact form -- a cell that
+                   provably lies inside the mesh is taken whole, any other cell is
+                   clipped by every tet within its reach (no tet_k heuristic, no
+                   candidate kNN).  Both agree when the candidate sets are complete. */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;
 
 /* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0,
- * whole_interior off (the reference's per-tet sums). */
+ * exact 0 (the reference's per-tet sums over tet_k candidates). */
 void vgb_config_init(vgb_config* cfg);
 
 /* One-line description of a CUDA device (name, SMs, memory) into buf. */

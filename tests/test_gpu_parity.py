@@ -211,14 +211,15 @@ def test_invalid_arguments_raise(built, meshgen):
         pkg.Engine(P.verts, P.tets, P.sites, site_k=200)  # above the supported maximum
 
 
-def test_whole_interior_cells_match_oracle(built, meshgen, oracle):
-    """Cells that provably lie inside the mesh are taken whole.  With complete
-    candidate sets (large tet_k) the reference's per-tet sums equal the whole
-    cells, so the oracle is the bar; boundary cells still go tet by tet."""
+def test_exact_form_matches_oracle(built, meshgen, oracle):
+    """Exact form: cells that provably lie inside the mesh are taken whole,
+    the others are clipped by every tet within reach.  With complete
+    candidate sets (large tet_k) the reference's per-tet sums are the exact
+    clipped cells, so the oracle run with that tet_k is the bar."""
     pkg = built
     P = meshgen.cube_problem(20, 20000, seed=1)
     tk = 100
-    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, whole_interior=True) as e:
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, exact=True) as e:
         e.iterate(1, update=False)
         e.sync()
         s4 = e.buffer("sites")
@@ -230,12 +231,12 @@ def test_whole_interior_cells_match_oracle(built, meshgen, oracle):
     check_moments(oracle, P, g, r)
 
 
-def test_whole_interior_on_torus(built, meshgen, oracle):
+def test_exact_form_on_torus(built, meshgen, oracle):
     """A non-convex mesh: the voxelised torus (32^3), uniform sites."""
     pkg = built
     P = meshgen.torus_problem(6000, grid=32, seed=4)
     tk = 100
-    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, whole_interior=True) as e:
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, exact=True) as e:
         e.iterate(1, update=False)
         e.sync()
         s4 = e.buffer("sites")
