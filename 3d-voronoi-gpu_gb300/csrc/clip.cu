@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
     const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
     const unsigned char* __restrict__ field, int fdim, const int* __restrict__ tet_order,
-    const int* __restrict__ tet_cell_start, int dim, float rt_max, const float* __restrict__ reach,
-    const unsigned* __restrict__ reach_max_bits) {
+    const int* __restrict__ tet_cell_start, int dim, float rt_max, const float4* __restrict__ tet_sph,
+    const float* __restrict__ reach, const unsigned* __restrict__ reach_max_bits) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -246,7 +246,16 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       const bool valid = idx < se;
       int t = -1;
       float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
-      if (valid) {
+      bool alive = valid;
+      if (exact && valid) {
+        // bounding spheres (the cell lies within Rc of its site), and the
+        // tet's reach: it has a site nearer than this one everywhere beyond
+        const float4 sp = tet_sph[idx];
+        const float ex = sp.x - seed.x, ey = sp.y - seed.y, ez = sp.z - seed.z;
+        const float dm = sqrtf(ex * ex + ey * ey + ez * ez);
+        alive = dm <= (Rc + sp.w) * 1.0001f + 1e-3f && dm <= reach[idx] * 1.0001f + 1e-2f;
+      }
+      if (alive) {
         t = exact ? tet_order[idx] : site_tets[idx];
         int4 q = tets[t];
         float4 a = verts[q.x], b = verts[q.y], cc = verts[q.z], d = verts[q.w];
@@ -255,19 +264,18 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         v2 = make_float3(cc.x - seed.x, cc.y - seed.y, cc.z - seed.z);
         v3 = make_float3(d.x - seed.x, d.y - seed.y, d.z - seed.z);
       }
-      bool alive = valid;
       if (CELL_TET) {
-        // bounding spheres: the cell lies within Rc of the site
-        const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
-                    mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
-        float rt2 = (v0.x - mx) * (v0.x - mx) + (v0.y - my) * (v0.y - my) + (v0.z - mz) * (v0.z - mz);
-        rt2 = fmaxf(rt2, (v1.x - mx) * (v1.x - mx) + (v1.y - my) * (v1.y - my) + (v1.z - mz) * (v1.z - mz));
-        rt2 = fmaxf(rt2, (v2.x - mx) * (v2.x - mx) + (v2.y - my) * (v2.y - my) + (v2.z - mz) * (v2.z - mz));
-        rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
-        const float dm = sqrtf(mx * mx + my * my + mz * mz);
-        if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
-        // exact form: the tet has a site nearer than this one everywhere
-        if (exact && valid && dm > reach[t] * 1.0001f + 1e-2f) alive = false;
+        if (!exact && alive) {
+          // bounding spheres: the cell lies within Rc of the site
+          const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
+                      mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
+          float rt2 = (v0.x - mx) * (v0.x - mx) + (v0.y - my) * (v0.y - my) + (v0.z - mz) * (v0.z - mz);
+          rt2 = fmaxf(rt2, (v1.x - mx) * (v1.x - mx) + (v1.y - my) * (v1.y - my) + (v1.z - mz) * (v1.z - mz));
+          rt2 = fmaxf(rt2, (v2.x - mx) * (v2.x - mx) + (v2.y - my) * (v2.y - my) + (v2.z - mz) * (v2.z - mz));
+          rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
+          const float dm = sqrtf(mx * mx + my * my + mz * mz);
+          if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
+        }
         // a tet whose four corners are strictly outside one face of the cell
         // cannot meet it
         for (int f = 0; f < nfaces; ++f) {
@@ -424,7 +432,7 @@ int clip_prepare() {
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
                     unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
-                    const int* tet_cell_start, int dim, float rt_max, const float* reach,
+                    const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
@@ -435,11 +443,11 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   if (cell_tet)
     k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
                                                             mom, stats, field, fdim, tet_order, tet_cell_start, dim,
-                                                            rt_max, reach, reach_max_bits);
+                                                            rt_max, tet_sph, reach, reach_max_bits);
   else
     k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
                                                              mom, stats, nullptr, 0, nullptr, nullptr, 0, 0.f, nullptr,
-                                                             nullptr);
+                                                             nullptr, nullptr);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

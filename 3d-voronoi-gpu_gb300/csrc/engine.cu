@@ -53,7 +53,8 @@ struct vgb_engine {
   unsigned char* field = nullptr;  // exact form: inside field of the mesh (else null)
   int fdim = 0;
   float rt_max = 0.f;              // exact form: largest tet corner distance from its centroid
-  float* reach = nullptr;          // exact form: per-tet reach (n_tet)
+  float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
+  float4* tet_sph = nullptr;       // exact form: tet bounding spheres (centroid-cell order)
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
@@ -160,7 +161,7 @@ void free_engine(vgb_engine* e) {
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
-                  e->io_stage, e->stats, e->field, e->reach, e->reach_max};
+                  e->io_stage, e->stats, e->field, e->reach, e->reach_max, e->tet_sph};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -180,8 +181,7 @@ int run_pass(vgb_engine* e, int update) {
   if (knn_sites(e->sites, e->n, e->dim, e->cell_start, e->K, e->pos_of_id, e->knn, st)) return VGB_ERR_CUDA;
   MARK(2);
   const bool exact = e->field != nullptr;
-  if (exact && tet_reach(e->sites, e->dim, e->cell_start, e->verts, e->tets, e->tet_order, e->n_tet, e->reach,
-                         e->reach_max, st))
+  if (exact && tet_reach(e->sites, e->dim, e->cell_start, e->tet_sph, e->n_tet, e->reach, e->reach_max, st))
     return VGB_ERR_CUDA;
   if (!exact &&
       knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
@@ -200,7 +200,7 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
                         e->site_start, e->site_tets, e->mom, e->stats, e->field, e->fdim,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->dim, e->rt_max,
-                        e->reach, e->reach_max, st))
+                        e->tet_sph, e->reach, e->reach_max, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -388,10 +388,11 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     }
     e->rt_max = rt * 1.001f + 1e-3f;
     if ((rc = dalloc(&e->field, field.size())) || (rc = dalloc(&e->reach, n_tet)) ||
-        (rc = dalloc(&e->reach_max, 1))) {
+        (rc = dalloc(&e->reach_max, 1)) || (rc = dalloc(&e->tet_sph, n_tet))) {
       free_engine(e);
       return rc;
     }
+    if (tet_spheres(e->verts, e->tets, e->tet_order, n_tet, e->tet_sph, e->st)) { free_engine(e); return VGB_ERR_CUDA; }
     ce = cudaMemcpy(e->field, field.data(), field.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   }

@@ -334,35 +334,22 @@ int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start
 }
 
 // ---------------------------------------------------------------------------
-// Reach of each tet (exact form): reach[t] = d1 + 2 r, d1 the distance from
-// its centroid to the nearest site, r its largest corner distance from the
-// centroid.  Every point x of the tet has a site within d1 + r, so a site s
-// whose cell meets the tet satisfies |s - centroid| <= reach[t].  The largest
+// Reach of each tet (exact form): reach[q] = d1 + 2 r for the tet at position
+// q of the centroid-cell order, d1 the distance from its centroid to the
+// nearest site, r the radius of its bounding sphere.  Every point x of the tet
+// has a site within d1 + r, so a site s whose cell meets the tet satisfies
+// |s - centroid| <= reach[q].  The largest
 // reach bounds every cell's search radius.  Thread per tet, in centroid-cell
 // order; a ring walk keeps the single nearest site.
 // ---------------------------------------------------------------------------
 __global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int* __restrict__ cell_start,
-                            const float4* __restrict__ verts, const int4* __restrict__ tets,
-                            const int* __restrict__ tet_order, int n_tet, float* __restrict__ reach,
+                            const float4* __restrict__ tet_sph, int n_tet, float* __restrict__ reach,
                             unsigned* __restrict__ reach_max_bits) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   float rr = 0.f;
   if (q < n_tet) {
-    const int t = tet_order[q];
-    const int4 v = tets[t];
-    const float4 a = verts[v.x], b = verts[v.y], c = verts[v.z], d = verts[v.w];
-    float4 Q;
-    Q.x = 0.25f * (a.x + b.x + c.x + d.x);
-    Q.y = 0.25f * (a.y + b.y + c.y + d.y);
-    Q.z = 0.25f * (a.z + b.z + c.z + d.z);
-    Q.w = 0.f;
-    float r2 = 0.f;
-    const float4 cs[4] = {a, b, c, d};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float dx = cs[i].x - Q.x, dy = cs[i].y - Q.y, dz = cs[i].z - Q.z;
-      r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
-    }
+    const float4 sp = tet_sph[q];
+    const float4 Q = make_float4(sp.x, sp.y, sp.z, 0.f);
     const float h = 1000.f / (float)dim;
     const int ci = grid_axis(Q.x, dim), cj = grid_axis(Q.y, dim), ck = grid_axis(Q.z, dim);
     float best = FLT_MAX;
@@ -393,8 +380,8 @@ __global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int
         }
       }
     }
-    rr = (sqrtf(best) + 2.f * sqrtf(r2)) * 1.0001f + 1e-3f;
-    reach[t] = rr;
+    rr = (sqrtf(best) + 2.f * sp.w) * 1.0001f + 1e-3f;
+    reach[q] = rr;
   }
   // block max, then one atomic per block (non-negative floats order as ints)
   __shared__ float bmax[8];
@@ -409,12 +396,11 @@ __global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int
   }
 }
 
-int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* verts, const int4* tets,
-              const int* tet_order, int n_tet, float* reach, unsigned* reach_max_bits, cudaStream_t st) {
+int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* tet_sph, int n_tet, float* reach,
+              unsigned* reach_max_bits, cudaStream_t st) {
   VGB_CUDA_TRY(cudaMemsetAsync(reach_max_bits, 0, sizeof(unsigned), st));
   if (n_tet <= 0) return 0;
-  k_tet_reach<<<(n_tet + 255) / 256, 256, 0, st>>>(sites, dim, cell_start, verts, tets, tet_order, n_tet, reach,
-                                                   reach_max_bits);
+  k_tet_reach<<<(n_tet + 255) / 256, 256, 0, st>>>(sites, dim, cell_start, tet_sph, n_tet, reach, reach_max_bits);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -443,6 +429,33 @@ __global__ void k_tet_scatter(const int* __restrict__ tcell, int n_tet, const in
   if (t >= n_tet) return;
   int c = tcell[t];
   order[start[c] + atomicAdd(fill + c, 1)] = t;
+}
+
+// Bounding sphere (centroid, largest corner distance) of each tet, in
+// centroid-cell order (exact form, once per mesh).
+__global__ void k_tet_spheres(const float4* __restrict__ verts, const int4* __restrict__ tets,
+                              const int* __restrict__ tet_order, int n_tet, float4* __restrict__ sph) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n_tet) return;
+  const int4 v = tets[tet_order[q]];
+  const float4 a = verts[v.x], b = verts[v.y], c = verts[v.z], d = verts[v.w];
+  const float cx = 0.25f * (a.x + b.x + c.x + d.x), cy = 0.25f * (a.y + b.y + c.y + d.y),
+              cz = 0.25f * (a.z + b.z + c.z + d.z);
+  float r2 = 0.f;
+  const float4 cs[4] = {a, b, c, d};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float dx = cs[i].x - cx, dy = cs[i].y - cy, dz = cs[i].z - cz;
+    r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+  }
+  sph[q] = make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + 1e-3f);
+}
+
+int tet_spheres(const float4* verts, const int4* tets, const int* tet_order, int n_tet, float4* sph, cudaStream_t st) {
+  if (n_tet <= 0) return 0;
+  k_tet_spheres<<<(n_tet + 255) / 256, 256, 0, st>>>(verts, tets, tet_order, n_tet, sph);
+  VGB_CUDA_TRY(cudaGetLastError());
+  return 0;
 }
 
 int tets_by_cell(const float4* verts, const int4* tets, int n_tet, int dim, int* tet_cell_start, int* cell_fill,

@@ -120,11 +120,14 @@ int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k,
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, cudaStream_t st);
-// Exact form: reach[t] = (distance from the centroid of t to its nearest
-// site) + 2 (largest corner distance from the centroid); *reach_max_bits =
-// float bits of the largest reach.  Sites must be grid-sorted.
-int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* verts, const int4* tets,
-              const int* tet_order, int n_tet, float* reach, unsigned* reach_max_bits, cudaStream_t st);
+// Exact form: reach[q] = (distance from the centroid of the q-th tet in
+// centroid-cell order to its nearest site) + 2 (its bounding radius);
+// *reach_max_bits = float bits of the largest reach.  Sites grid-sorted,
+// tet_sph from tet_spheres.
+int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* tet_sph, int n_tet, float* reach,
+              unsigned* reach_max_bits, cudaStream_t st);
+// Bounding spheres (centroid, radius) of the tets in centroid-cell order.
+int tet_spheres(const float4* verts, const int4* tets, const int* tet_order, int n_tet, float4* sph, cudaStream_t st);
 // Tets sorted by the grid cell of their float32 centroid (once per mesh):
 // tet_cell_start dim^3 + 1 ints, cell_fill dim^3 scratch, tcell n_tet scratch,
 // tet_order n_tet ints.
@@ -147,7 +150,7 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
                     unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
-                    const int* tet_cell_start, int dim, float rt_max, const float* reach,
+                    const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
