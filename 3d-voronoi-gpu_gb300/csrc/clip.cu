@@ -72,30 +72,19 @@ struct SiteSmem {
   float mr2;
 };
 
-// Apply planes 4+j (bisectors, nearest first) until the security radius is
-// reached (voronoi.cu:679-697).  Returns 0 ok, 1 empty, 2 failed; *secmiss
-// is set when every neighbour was used without reaching it.
-__device__ __forceinline__ int clip_by_bisectors(WarpCell& c, SiteSmem& S, int K, int lane, bool& secmiss) {
-  secmiss = false;
-  for (int j = 0; j < K; ++j) {
-    const float4 P = S.plane[4 + j];
-    if (lane == 0) { S.cnt[WC_PLANES]++; S.cnt[WC_CONFLICT] += (unsigned)c.nt; }
-    const int r = warp_clip(c, P, (unsigned)(4 + j), S.plane, S.conf, S.bedge, lane);
-    if (r == CLIP_EMPTY) return 1;
-    if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
-      if (lane == 0) S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
-      return 2;
-    }
-    if (r == CLIP_CUT && lane == 0) S.cnt[WC_CLIPS]++;
-    if (2.f * P.w > 4.f * c.r2) return 0;  // |neighbour - site|^2 > 4 max|v - site|^2
-  }
-  // every neighbour used: final check on the K-th (voronoi.cu:693-697)
-  secmiss = !(2.f * S.plane[4 + K - 1].w > 4.f * c.r2);
-  return 0;
-}
-
+// One kernel body, one copy of the clip and of the moments: every cell of a
+// site -- the cell built from the bisectors (cell-tet method) and each
+// candidate tet's cell -- goes through the same plane loop and the same
+// moment step, driven as a small state machine.  The clip is the bulk of the
+// code; a single copy keeps the hot loop inside the instruction cache.
+//
+// Plane sequences (ids index SiteSmem::plane):
+//   * bisectors 4 .. 4+K-1, nearest first, until the security radius is
+//     reached (voronoi.cu:679-697): the cell-tet build and the tet-cell
+//     method's per-tet cells;
+//   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
 template <bool CELL_TET>
-__global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, int K,
     const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
     const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
@@ -109,6 +98,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   if (lane < WC_N) S.cnt[lane] = 0u;
   unsigned cull_lane = 0;  // per-lane tet-vs-plane tests of the culling pass
+  const bool exact = CELL_TET && tet_order != nullptr;
   __syncwarp();
 
   for (int s = blockIdx.x * CLIP_WARPS + wib; s < n; s += gridDim.x * CLIP_WARPS) {
@@ -120,207 +110,154 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
       S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
     }
-    float Rc = 0.f;
-    int nfaces = 0;
-    bool cell_ok = true, interior = false;
-    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
+    // The reference starts the cell-tet cell from the box [-0.1, 1000.1]^3
+    // (voronoi.cu:125-161).  Here it starts from a cube centred on the site
+    // that contains that box: every tet lies inside both, so the cell clipped
+    // by a tet is the same, and the cube's edges are in general position (an
+    // edge of the fixed box can lie exactly on mesh planes such as x = y,
+    // where float rounding then splits the edge).
+    float L = 0.f;
     if (CELL_TET) {
-      // The reference starts the cell from the box [-0.1, 1000.1]^3
-      // (voronoi.cu:125-161).  Here it starts from a cube centred on the site
-      // that contains that box: every tet lies inside both, so the cell
-      // clipped by a tet is the same, and the cube's edges are in general
-      // position (an edge of the fixed box can lie exactly on mesh planes
-      // such as x = y, where float rounding then splits the edge).
       const float lo = -0.1f, hi = 1000.1f;
-      const float L = fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
-                            fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
+      L = fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
+                fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
       if (lane < BOX_PLANES) {
         const int ax = lane >> 1;
         const float sgn = (lane & 1) ? -1.f : 1.f;
         S.plane[4 + K + lane] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
       }
-      __syncwarp();
-      WarpCell c;
-      cell_clear(c);
-      if (lane < 8) {
-        // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
-        // ordered so each dual triangle has a negative normal determinant
-        const unsigned bx = lane & 1, by = (lane >> 1) & 1, bz = (lane >> 2) & 1;
-        const unsigned fx = 4 + K + bx, fy = 4 + K + 2 + by, fz = 4 + K + 4 + bz;
-        c.tri[0] = ((bx ^ by ^ bz) & 1) ? pack_tri(fx, fy, fz) : pack_tri(fx, fz, fy);
-        c.vx[0] = bx ? L : -L;
-        c.vy[0] = by ? L : -L;
-        c.vz[0] = bz ? L : -L;
-        c.vw[0] = 3.f * L * L;
-      }
-      c.vm[0] = 0xffu;
-      c.nt = 8;
-      c.r2 = warp_max(lane < 8 ? c.vw[0] : 0.f);
-      __syncwarp();
-      bool secmiss = false;
-      const int r = clip_by_bisectors(c, S, K, lane, secmiss);
-      cell_ok = (r == 0);
-      if (secmiss && lane == 0) S.cnt[WC_SECMISS]++;
-#pragma unroll
-      for (int k = 0; k < TRI_SLOTS; ++k)
-        if (c.vm[k] & lane_bit) {
-          S.mtri[k * WARP + lane] = c.tri[k];
-          S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
-        }
-      if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
-      if (lane == 0) { S.mnt = c.nt; S.mr2 = c.r2; }
-      Rc = sqrtf(c.r2);
-      // A cell that provably lies inside the mesh is its own clipped cell:
-      // the sum over the tets it meets of (cell ^ tet) is the cell itself.
-      // field[f] = d > 0 marks an inside cell of the field grid whose points
-      // are at least (d - 1) * h from the mesh boundary; the cell lies
-      // within Rc of its site.
-      if (field && cell_ok && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
-          seed.y <= 1000.f && seed.z >= 0.f && seed.z <= 1000.f) {
-        const int fc = grid_cell(seed.x, seed.y, seed.z, fdim);
-        const int fd = field[fc];
-        const float fh = 1000.f / (float)fdim;
-        if (fd >= 2 && (float)(fd - 1) * fh > Rc * 1.001f + 0.01f) {
-          float vol, mx, my, mz;
-          warp_moments(c, S.plane, lane, vol, mx, my, mz);
-          if (lane == 0) {
-            V.add(vol);
-            MX.add(mx);
-            MY.add(my);
-            MZ.add(mz);
-            S.cnt[WC_INTERIOR]++;
-            S.cnt[WC_FINAL] += (unsigned)c.nt;
-          }
-          interior = true;
-        }
-      }
-      // the planes that bound the cell (ids present in its triangles)
-      unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
-#pragma unroll
-      for (int k = 0; k < TRI_SLOTS; ++k)
-        if (c.vm[k] & lane_bit)
-#pragma unroll
-          for (int e = 0; e < 3; ++e) {
-            const unsigned id = tri_at(c.tri[k], e);
-            pm[id >> 5] |= 1u << (id & 31u);
-          }
-      nfaces = 0;
-#pragma unroll
-      for (int w = 0; w < 5; ++w) {
-        const unsigned word = __reduce_or_sync(FULL, pm[w]);
-        const bool has = (word >> lane) & 1u;
-        const unsigned hm = __ballot_sync(FULL, has);
-        if (has) S.faces[nfaces + __popc(hm & lt_mask)] = (unsigned char)(w * 32 + lane);
-        nfaces += __popc(hm);
-      }
     }
     __syncwarp();
-    // Candidate tets, as segments of a list: the site's candidate list (the
-    // reference's tet_k sets), or, in the exact form, the x-runs of
-    // centroid-grid cells within reach of the cell -- a tet meeting the cell
-    // has its centroid within Rc + rt_max of the site.
-    const bool exact = tet_order != nullptr;
-    int nseg = 1, nj = 1, i0 = 0, i1 = 0, j0 = 0, k0 = 0;
-    if (exact && cell_ok && !interior) {
-      // no cell reaches a tet whose centroid is farther than the largest reach
-      const float R = fminf(Rc + rt_max * 1.001f, __uint_as_float(*reach_max_bits)) + 0.01f;
-      i0 = grid_axis(seed.x - R, dim);
-      i1 = grid_axis(seed.x + R, dim);
-      j0 = grid_axis(seed.y - R, dim);
-      k0 = grid_axis(seed.z - R, dim);
-      nj = grid_axis(seed.y + R, dim) - j0 + 1;
-      nseg = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
-    }
-    for (int q = 0; cell_ok && !interior && q < nseg; ++q) {
-    int sb, se;
-    if (exact) {
-      const int row = dim * ((j0 + q % nj) + dim * (k0 + q / nj));
-      sb = tet_cell_start[i0 + row];
-      se = tet_cell_start[i1 + row + 1];
-    } else {
-      sb = site_start[s];
-      se = site_start[s + 1];
-    }
-    for (int base = sb; base < se; base += WARP) {
-      const int idx = base + lane;
-      const bool valid = idx < se;
-      int t = -1;
-      float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
-      bool alive = valid;
-      if (exact && valid) {
-        // bounding spheres (the cell lies within Rc of its site), and the
-        // tet's reach: it has a site nearer than this one everywhere beyond
-        const float4 sp = tet_sph[idx];
-        const float ex = sp.x - seed.x, ey = sp.y - seed.y, ez = sp.z - seed.z;
-        const float dm = sqrtf(ex * ex + ey * ey + ez * ez);
-        alive = dm <= (Rc + sp.w) * 1.0001f + 1e-3f && dm <= reach[idx] * 1.0001f + 1e-2f;
-      }
-      if (alive) {
-        t = exact ? tet_order[idx] : site_tets[idx];
-        int4 q = tets[t];
-        float4 a = verts[q.x], b = verts[q.y], cc = verts[q.z], d = verts[q.w];
-        v0 = make_float3(a.x - seed.x, a.y - seed.y, a.z - seed.z);
-        v1 = make_float3(b.x - seed.x, b.y - seed.y, b.z - seed.z);
-        v2 = make_float3(cc.x - seed.x, cc.y - seed.y, cc.z - seed.z);
-        v3 = make_float3(d.x - seed.x, d.y - seed.y, d.z - seed.z);
-      }
-      if (CELL_TET) {
-        if (!exact && alive) {
-          // bounding spheres: the cell lies within Rc of the site
-          const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
-                      mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
-          float rt2 = (v0.x - mx) * (v0.x - mx) + (v0.y - my) * (v0.y - my) + (v0.z - mz) * (v0.z - mz);
-          rt2 = fmaxf(rt2, (v1.x - mx) * (v1.x - mx) + (v1.y - my) * (v1.y - my) + (v1.z - mz) * (v1.z - mz));
-          rt2 = fmaxf(rt2, (v2.x - mx) * (v2.x - mx) + (v2.y - my) * (v2.y - my) + (v2.z - mz) * (v2.z - mz));
-          rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
-          const float dm = sqrtf(mx * mx + my * my + mz * mz);
-          if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
+
+    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
+    float Rc = 0.f;
+    int nfaces = 0;
+    bool building = CELL_TET;  // the current cell is the site's own cell
+    // candidate scan: segments of a tet list, 32 tets per chunk
+    int nseg = 0, nj = 1, i0 = 0, i1 = 0, j0 = 0, k0 = 0;
+    int seg = -1, base = 0, se = 0, qi = 0, nsurv = 0;
+    if (!CELL_TET) nseg = 1;
+
+    while (true) {
+      // ---------------------------------------------------------------
+      // the next cell: the site's cell, or the next surviving candidate
+      WarpCell c;
+      cell_clear(c);
+      if (building) {
+        if (lane < 8) {
+          // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
+          // ordered so each dual triangle has a negative normal determinant
+          const unsigned bx = lane & 1, by = (lane >> 1) & 1, bz = (lane >> 2) & 1;
+          const unsigned fx = 4 + K + bx, fy = 4 + K + 2 + by, fz = 4 + K + 4 + bz;
+          c.tri[0] = ((bx ^ by ^ bz) & 1) ? pack_tri(fx, fy, fz) : pack_tri(fx, fz, fy);
+          c.vx[0] = bx ? L : -L;
+          c.vy[0] = by ? L : -L;
+          c.vz[0] = bz ? L : -L;
+          c.vw[0] = 3.f * L * L;
         }
-        // a tet whose four corners are strictly outside one face of the cell
-        // cannot meet it
-        for (int f = 0; f < nfaces; ++f) {
-          if (!__any_sync(FULL, alive)) break;
-          const float4 P = S.plane[S.faces[f]];
-          if (alive) {
-            ++cull_lane;
-            if (plane_eval(P, v0.x, v0.y, v0.z) < 0.f && plane_eval(P, v1.x, v1.y, v1.z) < 0.f &&
-                plane_eval(P, v2.x, v2.y, v2.z) < 0.f && plane_eval(P, v3.x, v3.y, v3.z) < 0.f)
-              alive = false;
-          }
-        }
+        c.vm[0] = 0xffu;
+        c.nt = 8;
+        c.r2 = 3.f * L * L;
       } else {
-        // one-plane separation: all four corners strictly outside a bisector.
-        // Planes come nearest first; none can separate once its distance
-        // exceeds the tet's farthest corner.
-        const float far2 = fmaxf(fmaxf(v0.x * v0.x + v0.y * v0.y + v0.z * v0.z, v1.x * v1.x + v1.y * v1.y + v1.z * v1.z),
-                                 fmaxf(v2.x * v2.x + v2.y * v2.y + v2.z * v2.z, v3.x * v3.x + v3.y * v3.y + v3.z * v3.z));
-        bool open = valid;
-        for (int j = 0; j < K; ++j) {
-          if (!__any_sync(FULL, open)) break;
-          const float4 P = S.plane[4 + j];
-          if (open) {
-            ++cull_lane;
-            if (2.f * P.w > 4.f * far2 * 1.0001f + 1e-6f) {
-              open = false;
-            } else if (plane_eval(P, v0.x, v0.y, v0.z) < 0.f && plane_eval(P, v1.x, v1.y, v1.z) < 0.f &&
-                       plane_eval(P, v2.x, v2.y, v2.z) < 0.f && plane_eval(P, v3.x, v3.y, v3.z) < 0.f) {
-              alive = false;
-              open = false;
+        // refill the queue from the next chunk(s) of candidates
+        while (qi >= nsurv) {
+          if (base >= se) {
+            if (++seg >= nseg) break;
+            if (exact) {
+              const int row = dim * ((j0 + seg % nj) + dim * (k0 + seg / nj));
+              base = tet_cell_start[i0 + row];
+              se = tet_cell_start[i1 + row + 1];
+            } else {
+              base = site_start[s];
+              se = site_start[s + 1];
+            }
+            continue;
+          }
+          const int idx = base + lane;
+          const bool valid = idx < se;
+          int t = -1;
+          float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
+          bool alive = valid;
+          if (exact && valid) {
+            // bounding spheres (the cell lies within Rc of its site), and the
+            // tet's reach: it has a site nearer than this one everywhere
+            // beyond
+            const float4 sp = tet_sph[idx];
+            const float ex = sp.x - seed.x, ey = sp.y - seed.y, ez = sp.z - seed.z;
+            const float dm = sqrtf(ex * ex + ey * ey + ez * ez);
+            alive = dm <= (Rc + sp.w) * 1.0001f + 1e-3f && dm <= reach[idx] * 1.0001f + 1e-2f;
+          }
+          if (alive) {
+            t = exact ? tet_order[idx] : site_tets[idx];
+            const int4 q = tets[t];
+            const float4 a = verts[q.x], b = verts[q.y], cc = verts[q.z], d = verts[q.w];
+            v0 = make_float3(a.x - seed.x, a.y - seed.y, a.z - seed.z);
+            v1 = make_float3(b.x - seed.x, b.y - seed.y, b.z - seed.z);
+            v2 = make_float3(cc.x - seed.x, cc.y - seed.y, cc.z - seed.z);
+            v3 = make_float3(d.x - seed.x, d.y - seed.y, d.z - seed.z);
+          }
+          if (CELL_TET) {
+            if (!exact && alive) {
+              // bounding spheres: the cell lies within Rc of the site
+              const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
+                          mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
+              float rt2 = (v0.x - mx) * (v0.x - mx) + (v0.y - my) * (v0.y - my) + (v0.z - mz) * (v0.z - mz);
+              rt2 = fmaxf(rt2, (v1.x - mx) * (v1.x - mx) + (v1.y - my) * (v1.y - my) + (v1.z - mz) * (v1.z - mz));
+              rt2 = fmaxf(rt2, (v2.x - mx) * (v2.x - mx) + (v2.y - my) * (v2.y - my) + (v2.z - mz) * (v2.z - mz));
+              rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
+              const float dm = sqrtf(mx * mx + my * my + mz * mz);
+              if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
+            }
+            // a tet whose four corners are strictly outside one face of the
+            // cell cannot meet it
+            for (int f = 0; f < nfaces; ++f) {
+              if (!__any_sync(FULL, alive)) break;
+              const float4 P = S.plane[S.faces[f]];
+              if (alive) {
+                ++cull_lane;
+                if (plane_eval(P, v0.x, v0.y, v0.z) < 0.f && plane_eval(P, v1.x, v1.y, v1.z) < 0.f &&
+                    plane_eval(P, v2.x, v2.y, v2.z) < 0.f && plane_eval(P, v3.x, v3.y, v3.z) < 0.f)
+                  alive = false;
+              }
+            }
+          } else {
+            // one-plane separation: all four corners strictly outside a
+            // bisector.  Planes come nearest first; none can separate once
+            // its distance exceeds the tet's farthest corner.
+            const float far2 =
+                fmaxf(fmaxf(v0.x * v0.x + v0.y * v0.y + v0.z * v0.z, v1.x * v1.x + v1.y * v1.y + v1.z * v1.z),
+                      fmaxf(v2.x * v2.x + v2.y * v2.y + v2.z * v2.z, v3.x * v3.x + v3.y * v3.y + v3.z * v3.z));
+            bool open = valid;
+            for (int j = 0; j < K; ++j) {
+              if (!__any_sync(FULL, open)) break;
+              const float4 P = S.plane[4 + j];
+              if (open) {
+                ++cull_lane;
+                if (2.f * P.w > 4.f * far2 * 1.0001f + 1e-6f) {
+                  open = false;
+                } else if (plane_eval(P, v0.x, v0.y, v0.z) < 0.f && plane_eval(P, v1.x, v1.y, v1.z) < 0.f &&
+                           plane_eval(P, v2.x, v2.y, v2.z) < 0.f && plane_eval(P, v3.x, v3.y, v3.z) < 0.f) {
+                  alive = false;
+                  open = false;
+                }
+              }
             }
           }
+          const unsigned survivors = __ballot_sync(FULL, alive);
+          const int nvalid = min(WARP, se - base);
+          nsurv = __popc(survivors);
+          qi = 0;
+          if (alive) S.queue[__popc(survivors & lt_mask)] = (unsigned)t;
+          if (lane == 0) {
+            S.cnt[WC_CAND] += (unsigned)nvalid;
+            S.cnt[WC_CULLED] += (unsigned)(nvalid - nsurv);
+            S.cnt[WC_CLIPPED] += (unsigned)nsurv;
+          }
+          base += WARP;
+          __syncwarp();
         }
-      }
-      const unsigned survivors = __ballot_sync(FULL, alive);
-      const int nvalid = min(WARP, se - base), nsurv = __popc(survivors);
-      if (alive) S.queue[__popc(survivors & lt_mask)] = (unsigned)t;
-      if (lane == 0) {
-        S.cnt[WC_CAND] += (unsigned)nvalid;
-        S.cnt[WC_CULLED] += (unsigned)(nvalid - nsurv);
-        S.cnt[WC_CLIPPED] += (unsigned)nsurv;
-      }
-      __syncwarp();
-      for (int qi = 0; qi < nsurv; ++qi) {
-        const int tq = (int)S.queue[qi];
+        if (qi >= nsurv) break;  // no candidate left
+        const int tq = (int)S.queue[qi++];
         if (lane < 4) {
           const int4 q = tets[tq];
           const int vi = lane == 0 ? q.x : lane == 1 ? q.y : lane == 2 ? q.z : q.w;
@@ -330,76 +267,146 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         __syncwarp();
         if (lane < 4) {
           // faces (c,b,d), (a,c,d), (b,a,d), (a,b,c) (voronoi.cu:179)
-          const int i0 = lane == 0 ? 2 : lane == 1 ? 0 : lane == 2 ? 1 : 0;
-          const int i1 = lane == 0 ? 1 : lane == 1 ? 2 : lane == 2 ? 0 : 1;
-          const int i2 = lane == 3 ? 2 : 3;
-          const float4 p0 = S.corner[i0], p1 = S.corner[i1], p2 = S.corner[i2];
+          const int f0 = lane == 0 ? 2 : lane == 1 ? 0 : lane == 2 ? 1 : 0;
+          const int f1 = lane == 0 ? 1 : lane == 1 ? 2 : lane == 2 ? 0 : 1;
+          const int f2 = lane == 3 ? 2 : 3;
+          const float4 p0 = S.corner[f0], p1 = S.corner[f1], p2 = S.corner[f2];
           S.plane[lane] = face_plane(make_float3(p0.x, p0.y, p0.z), make_float3(p1.x, p1.y, p1.z),
                                      make_float3(p2.x, p2.y, p2.z));
         }
-        WarpCell c;
-        cell_clear(c);
         if (CELL_TET) {
 #pragma unroll
           for (int k = 0; k < TRI_SLOTS; ++k) {
             c.vm[k] = S.mvm[k];
             if (c.vm[k] & lane_bit) {
               c.tri[k] = S.mtri[k * WARP + lane];
-              const float4 q = S.mv[k * WARP + lane];
-              c.vx[k] = q.x; c.vy[k] = q.y; c.vz[k] = q.z; c.vw[k] = q.w;
+              const float4 v = S.mv[k * WARP + lane];
+              c.vx[k] = v.x; c.vy[k] = v.y; c.vz[k] = v.z; c.vw[k] = v.w;
             }
           }
           c.nt = S.mnt;
           c.r2 = S.mr2;
-        } else if (lane < 4) {
-          // the tet's corners as triangles of their three faces: a, d, c, b
-          const float4 p = S.corner[lane == 0 ? 0 : lane == 1 ? 3 : lane == 2 ? 2 : 1];
-          c.tri[0] = lane == 0 ? pack_tri(1, 3, 2) : lane == 1 ? pack_tri(0, 1, 2) : lane == 2 ? pack_tri(0, 3, 1)
-                                                                                               : pack_tri(0, 2, 3);
-          c.vx[0] = p.x; c.vy[0] = p.y; c.vz[0] = p.z;
-          c.vw[0] = p.x * p.x + p.y * p.y + p.z * p.z;
-        }
-        if (!CELL_TET) {
+        } else {
+          if (lane < 4) {
+            // the tet's corners as triangles of their three faces: a, d, c, b
+            const float4 p = S.corner[lane == 0 ? 0 : lane == 1 ? 3 : lane == 2 ? 2 : 1];
+            c.tri[0] = lane == 0 ? pack_tri(1, 3, 2) : lane == 1 ? pack_tri(0, 1, 2)
+                     : lane == 2 ? pack_tri(0, 3, 1) : pack_tri(0, 2, 3);
+            c.vx[0] = p.x; c.vy[0] = p.y; c.vz[0] = p.z;
+            c.vw[0] = p.x * p.x + p.y * p.y + p.z * p.z;
+          }
           c.vm[0] = 0xfu;
           c.nt = 4;
           c.r2 = warp_max(lane < 4 ? c.vw[0] : 0.f);
         }
         __syncwarp();
-        int state = 0;  // 0 contributes, 1 empty, 2 dropped
-        if (CELL_TET) {
-          for (int f = 0; f < 4; ++f) {
-            if (lane == 0) { S.cnt[WC_PLANES]++; S.cnt[WC_CONFLICT] += (unsigned)c.nt; }
-            const int r = warp_clip(c, S.plane[f], (unsigned)f, S.plane, S.conf, S.bedge, lane);
-            if (r == CLIP_EMPTY) { state = 1; break; }
-            if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
-              if (lane == 0) S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
-              state = 2;
-              break;
-            }
-            if (r == CLIP_CUT && lane == 0) S.cnt[WC_CLIPS]++;
-          }
-        } else {
-          bool secmiss = false;
-          const int r = clip_by_bisectors(c, S, K, lane, secmiss);
-          state = r;
-          if (secmiss && lane == 0) S.cnt[WC_SECMISS]++;
+      }
+
+      // ---------------------------------------------------------------
+      // the plane sequence: bisectors until the security radius, or the
+      // tet's four faces
+      const bool bis = building || !CELL_TET;
+      const int pend = bis ? 4 + K : 4;
+      int state = 0;  // 0 kept, 1 empty, 2 dropped
+      bool secmiss = bis;
+      for (int pi = bis ? 4 : 0; pi < pend; ++pi) {
+        const float4 P = S.plane[pi];
+        if (lane == 0) { S.cnt[WC_PLANES]++; S.cnt[WC_CONFLICT] += (unsigned)c.nt; }
+        const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane);
+        if (r == CLIP_EMPTY) { state = 1; break; }
+        if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
+          if (lane == 0) S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
+          state = 2;
+          break;
         }
-        if (state == 1) { if (lane == 0) S.cnt[WC_EMPTY]++; }
-        if (state == 0) {
-          float vol, mx, my, mz;
-          warp_moments(c, S.plane, lane, vol, mx, my, mz);
-          if (lane == 0) {
-            V.add(vol);
-            MX.add(mx);
-            MY.add(my);
-            MZ.add(mz);
-            S.cnt[WC_CONTRIB]++;
-            S.cnt[WC_FINAL] += (unsigned)c.nt;
+        if (r == CLIP_CUT && lane == 0) S.cnt[WC_CLIPS]++;
+        // |neighbour - site|^2 > 4 max|v - site|^2
+        if (bis && 2.f * P.w > 4.f * c.r2) { secmiss = false; break; }
+      }
+      if (bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
+
+      // ---------------------------------------------------------------
+      bool take = state == 0, interior = false;
+      if (building) {
+        building = false;
+        take = false;
+        if (state != 0) break;  // the site's cell failed: no tet is clipped
+#pragma unroll
+        for (int k = 0; k < TRI_SLOTS; ++k)
+          if (c.vm[k] & lane_bit) {
+            S.mtri[k * WARP + lane] = c.tri[k];
+            S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
+          }
+        if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
+        if (lane == 0) { S.mnt = c.nt; S.mr2 = c.r2; }
+        Rc = sqrtf(c.r2);
+        // A cell that provably lies inside the mesh is its own clipped cell:
+        // the sum over the tets it meets of (cell ^ tet) is the cell itself.
+        // field[f] = d > 0 marks an inside cell of the field grid whose
+        // points are at least (d - 1) * h from the mesh boundary; the cell
+        // lies within Rc of its site.
+        if (field && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f && seed.y <= 1000.f &&
+            seed.z >= 0.f && seed.z <= 1000.f) {
+          const int fd = field[grid_cell(seed.x, seed.y, seed.z, fdim)];
+          const float fh = 1000.f / (float)fdim;
+          interior = fd >= 2 && (float)(fd - 1) * fh > Rc * 1.001f + 0.01f;
+        }
+        take = interior;
+        if (!interior) {
+          // the planes that bound the cell (ids present in its triangles)
+          unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+          for (int k = 0; k < TRI_SLOTS; ++k)
+            if (c.vm[k] & lane_bit)
+#pragma unroll
+              for (int e = 0; e < 3; ++e) {
+                const unsigned id = tri_at(c.tri[k], e);
+                pm[id >> 5] |= 1u << (id & 31u);
+              }
+          nfaces = 0;
+#pragma unroll
+          for (int w = 0; w < 5; ++w) {
+            const unsigned word = __reduce_or_sync(FULL, pm[w]);
+            const bool has = (word >> lane) & 1u;
+            const unsigned hm = __ballot_sync(FULL, has);
+            if (has) S.faces[nfaces + __popc(hm & lt_mask)] = (unsigned char)(w * 32 + lane);
+            nfaces += __popc(hm);
+          }
+          // candidate tets: the site's candidate list (the reference's tet_k
+          // sets), or, in the exact form, the x-runs of centroid-grid cells
+          // within reach of the cell -- a tet meeting the cell has its
+          // centroid within Rc + rt_max of the site, and no tet reaches
+          // farther than the largest reach
+          if (exact) {
+            const float R = fminf(Rc + rt_max * 1.001f, __uint_as_float(*reach_max_bits)) + 0.01f;
+            i0 = grid_axis(seed.x - R, dim);
+            i1 = grid_axis(seed.x + R, dim);
+            j0 = grid_axis(seed.y - R, dim);
+            k0 = grid_axis(seed.z - R, dim);
+            nj = grid_axis(seed.y + R, dim) - j0 + 1;
+            nseg = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
+          } else {
+            nseg = 1;
           }
         }
         __syncwarp();
       }
-    }
+      if (take) {
+        float vol, mx, my, mz;
+        warp_moments(c, S.plane, lane, vol, mx, my, mz);
+        if (lane == 0) {
+          V.add(vol);
+          MX.add(mx);
+          MY.add(my);
+          MZ.add(mz);
+          S.cnt[interior ? WC_INTERIOR : WC_CONTRIB]++;
+          S.cnt[WC_FINAL] += (unsigned)c.nt;
+        }
+      } else if (state == 1 && lane == 0) {
+        S.cnt[WC_EMPTY]++;
+      }
+      __syncwarp();
+      if (interior) break;
     }
     if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
     __syncwarp();

@@ -15,88 +15,36 @@
 // Distances are fma(dz,dz, fma(dy,dy, dx*dx)) in float, as nvcc evaluates the
 // reference's expressions.
 //
-// Layout: one CTA per segment of SEG_W grid cells along x (fixed y, z).  Its
-// queries are the sites (or tet centroids, pre-sorted by cell once per mesh)
-// of those cells, one thread each.  The CTA stages every site of the cells
-// within STAGE_R rings of the segment into shared memory with coalesced loads
-// ((2R+1)^2 contiguous x-runs of the sorted array), so all queries scan their
-// (2R+1)^3 neighbourhood from shared memory.  Each thread keeps its K best as
-// a max-heap of 64-bit keys (distance bits << 32 | id) in shared memory; the
-// heap root (the current k-th key) stays in a register, so rejecting a
-// candidate is one compare.  A query whose k-th distance is not below the
-// distance to every unstaged cell continues the ring walk from global memory,
-// as do all queries of a segment whose neighbourhood does not fit.
+// Layout: one warp per query; consecutive warps take consecutive queries in
+// grid order, so the warps of a CTA read the same cells (L1 reuse).  The
+// warp visits the grid cells around the query's cell in Chebyshev shells
+// (the cell, then the 26 around it, ...), 32 cells at a time, one per lane;
+// a cell whose box is farther than the current k-th distance is skipped.
+// The sites of the kept cells are then scanned 32 at a time, one per lane
+// (a warp scan of the cell counts maps lane -> site).  Each candidate is a
+// 64-bit key (distance bits << 32 | id).  Keys below the current k-th key go
+// to a per-warp buffer in shared memory; 32 buffered keys are sorted with a
+// bitonic network across the lanes and merged into the warp's sorted list of
+// the best 32*S keys (S slots per lane, held in registers).  After each shell
+// the buffer is flushed, and the walk stops once the k-th distance is below
+// the distance from the query to every cell beyond the shell.
 #include <cfloat>
 
 #include "vgb_common.cuh"
 
 namespace vgb {
 
-constexpr int KNN_THREADS = 64;
-constexpr int SEG_W = 2;             // cells per segment along x
-constexpr int STAGE_R = 2;           // staged rings around the segment
-constexpr int STAGE_CAP = 0;         // staged sites per CTA (0: rings are walked from global memory)
-constexpr int STAGE_ROWS = (2 * STAGE_R + 1) * (2 * STAGE_R + 1);
-constexpr int STAGE_ROW_CELLS = SEG_W + 2 * STAGE_R;
+constexpr int KNN_WARPS = 8;  // warps (queries in flight) per CTA
+constexpr int KNN_BUF = 64;   // per-warp key buffer
 constexpr float KNN_MARGIN = 0.01f;  // in [0,1000] units; cell-assignment rounding is ~1e-4
+constexpr unsigned KFULL = 0xffffffffu;
 
 typedef unsigned long long u64;
+constexpr u64 KEY_NONE = ~0ull;
 
 __device__ __forceinline__ u64 heap_key(float d, float4 p) {
   return ((u64)__float_as_uint(d) << 32) | (u64)(unsigned)site_id(p);
 }
-
-struct KnnHeap {
-  u64* h;    // h[j * KNN_THREADS]
-  int K, cnt;
-  u64 root;  // current k-th key once full, else ~0
-
-  __device__ u64& at(int j) { return h[j * KNN_THREADS]; }
-
-  __device__ void sift_down(int i, u64 x, int size) {
-    while (true) {
-      int l = 2 * i + 1;
-      if (l >= size) break;
-      int r = l + 1;
-      u64 hl = at(l);
-      int c = l;
-      if (r < size) {
-        u64 hr = at(r);
-        if (hr > hl) { c = r; hl = hr; }
-      }
-      if (hl <= x) break;
-      at(i) = hl;
-      i = c;
-    }
-    at(i) = x;
-  }
-
-  __device__ void push(u64 x) {
-    if (cnt < K) {
-      at(cnt++) = x;
-      if (cnt == K) {
-        for (int i = K / 2 - 1; i >= 0; --i) sift_down(i, at(i), K);
-        root = at(0);
-      }
-    } else if (x < root) {
-      sift_down(0, x, K);
-      root = at(0);
-    }
-  }
-
-  // ascending order in place (heapsort)
-  __device__ void sort() {
-    if (cnt < K) {
-      for (int i = cnt / 2 - 1; i >= 0; --i) sift_down(i, at(i), cnt);
-    }
-    for (int sz = cnt - 1; sz > 0; --sz) {
-      u64 top = at(0);
-      u64 x = at(sz);
-      at(sz) = top;
-      sift_down(0, x, sz);
-    }
-  }
-};
 
 __device__ __forceinline__ float box_d2(float4 Q, int i, int j, int k, int dim, float h) {
   float lo, hi;
@@ -125,173 +73,205 @@ __device__ __forceinline__ float ring_bound(float4 Q, int ci, int cj, int ck, in
   return L;
 }
 
-__device__ __forceinline__ bool done_after_ring(const KnnHeap& H, float4 Q, int ci, int cj, int ck, int r, int dim,
-                                                float h) {
-  if (H.cnt < H.K) return false;
-  float L = ring_bound(Q, ci, cj, ck, r, dim, h);
-  if (L == FLT_MAX) return true;
-  L -= KNN_MARGIN;
-  float kd = __uint_as_float((unsigned)(H.root >> 32));
-  return L > 0.f && kd < L * L;
-}
-
-// Ring walk from global memory over rings [r0, ...) until exact.
-__device__ void ring_walk(KnnHeap& H, float4 Q, int self, int ci, int cj, int ck, int r0, const float4* sites,
-                          const int* cell_start, int dim, float h) {
-  for (int r = r0;; ++r) {
-    bool left = (ci - r >= 0) || (ci + r <= dim - 1) || (cj - r >= 0) || (cj + r <= dim - 1) || (ck - r >= 0) ||
-                (ck + r <= dim - 1);
-    if (!left) break;
-    if (r > 0 && done_after_ring(H, Q, ci, cj, ck, r, dim, h)) break;
-    for (int dk = -r; dk <= r; ++dk) {
-      int k = ck + dk;
-      if (k < 0 || k >= dim) continue;
-      for (int dj = -r; dj <= r; ++dj) {
-        int j = cj + dj;
-        if (j < 0 || j >= dim) continue;
-        bool face = (dk == -r || dk == r || dj == -r || dj == r);
-        for (int di = -r; di <= r; di += (face || r == 0) ? 1 : 2 * r) {
-          int i = ci + di;
-          if (i < 0 || i >= dim) continue;
-          if (H.cnt == H.K &&
-              box_d2(Q, i, j, k, dim, h) > __uint_as_float((unsigned)(H.root >> 32)))
-            continue;
-          int c = i + dim * (j + dim * k);
-          int b = cell_start[c], e = cell_start[c + 1];
-          for (int p = b; p < e; ++p) {
-            if (p == self) continue;
-            float4 P = sites[p];
-            H.push(heap_key(dist2(Q, P), P));
-          }
-        }
-      }
-    }
+// Offset (di, dj, dk) of the t-th cell of Chebyshev shell w >= 1 (t below
+// (2w+1)^3 - (2w-1)^3): the two planes dk = -w, +w first, then for each
+// inner dk the ring of 8w cells.
+__device__ __forceinline__ void shell_cell(int w, int t, int& di, int& dj, int& dk) {
+  const int side = 2 * w + 1, plane = side * side;
+  if (t < 2 * plane) {
+    const int r = t % plane;
+    dk = t < plane ? -w : w;
+    di = r % side - w;
+    dj = r / side - w;
+    return;
+  }
+  t -= 2 * plane;
+  dk = t / (8 * w) - (w - 1);
+  const int u = t % (8 * w);
+  if (u < 2 * side) {
+    dj = u < side ? -w : w;
+    di = u % side - w;
+  } else {
+    const int v = u - 2 * side, inner = 2 * w - 1;
+    di = v < inner ? -w : w;
+    dj = v % inner - (w - 1);
   }
 }
 
-template <bool CENTROIDS>
-__global__ void __launch_bounds__(KNN_THREADS) k_knn(const float4* __restrict__ sites, int n, int dim,
-                                                     const int* __restrict__ cell_start, int K,
-                                                     const float4* __restrict__ verts,
-                                                     const int4* __restrict__ tets,
-                                                     const int* __restrict__ q_order,
-                                                     const int* __restrict__ q_cell_start,
-                                                     const int* __restrict__ pos_of_id,
-                                                     unsigned* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char knn_smem[];
-  float4* st_pts = reinterpret_cast<float4*>(knn_smem);                         // STAGE_CAP
-  u64* heap_base = reinterpret_cast<u64*>(st_pts + STAGE_CAP);                  // K * KNN_THREADS
-  __shared__ int st_row_off[STAGE_ROWS + 1];                                    // staged offset per row
-  __shared__ int st_cell[STAGE_ROWS][STAGE_ROW_CELLS + 1];                      // cell_start, row-relative
-  __shared__ int st_total;
+// Ascending bitonic sort of one key per lane.
+__device__ __forceinline__ u64 warp_sort32(u64 x, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const u64 y = __shfl_xor_sync(KFULL, x, j);
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      x = keep_min ? (x < y ? x : y) : (x < y ? y : x);
+    }
+  }
+  return x;
+}
 
-  const int tid = threadIdx.x;
-  const int nseg = (dim + SEG_W - 1) / SEG_W;
-  const int row = blockIdx.x / nseg;
-  const int j0 = row % dim, k0 = row / dim;
-  const int i0 = (blockIdx.x % nseg) * SEG_W;
-  const int i1 = min(i0 + SEG_W, dim) - 1;
-  const int* qcs = CENTROIDS ? q_cell_start : cell_start;
-  const int qb = qcs[i0 + dim * (j0 + dim * k0)];
-  const int qe = qcs[i1 + dim * (j0 + dim * k0) + 1];
-  if (qb >= qe) return;
+// Ascending order of a bitonic sequence of one key per lane.
+__device__ __forceinline__ u64 warp_clean32(u64 x, int lane) {
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const u64 y = __shfl_xor_sync(KFULL, x, j);
+    x = ((lane & j) == 0) ? (x < y ? x : y) : (x < y ? y : x);
+  }
+  return x;
+}
+
+// Merge 32 keys (one per lane, any order) into the ascending list L of
+// 32*S keys (entry s*32 + lane in L[s]), keeping the smallest 32*S.
+template <int S>
+__device__ __forceinline__ void warp_merge(u64 (&L)[S], u64 b, int lane) {
+  u64 c = warp_sort32(b, lane);
+  // the 32 smallest of the last slot and the buffer (a bitonic split)
+  u64 cr = __shfl_sync(KFULL, c, 31 - lane);
+  c = warp_clean32(L[S - 1] < cr ? L[S - 1] : cr, lane);
+#pragma unroll
+  for (int s = S - 2; s >= 0; --s) {
+    cr = __shfl_sync(KFULL, c, 31 - lane);
+    const u64 lo = L[s] < cr ? L[s] : cr, hi = L[s] < cr ? cr : L[s];
+    L[s + 1] = warp_clean32(hi, lane);
+    c = warp_clean32(lo, lane);
+  }
+  L[0] = c;
+}
+
+template <int S>
+__device__ __forceinline__ u64 kth_key(const u64 (&L)[S], int K) {
+  const int s = (K - 1) >> 5;
+  u64 v = L[0];
+#pragma unroll
+  for (int q = 1; q < S; ++q)
+    if (s == q) v = L[q];
+  return __shfl_sync(KFULL, v, (K - 1) & 31);
+}
+
+template <int S, bool CENTROIDS>
+__global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict__ sites, int n, int dim,
+                                                        const int* __restrict__ cell_start, int K,
+                                                        const float4* __restrict__ verts,
+                                                        const int4* __restrict__ tets,
+                                                        const int* __restrict__ q_order, int n_query,
+                                                        const int* __restrict__ pos_of_id,
+                                                        unsigned* __restrict__ out) {
+  __shared__ u64 buf_all[KNN_WARPS][KNN_BUF];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  u64* buf = buf_all[wib];
   const float h = 1000.f / (float)dim;
-  const int xa = max(0, i0 - STAGE_R), xb = min(dim - 1, i1 + STAGE_R);
-
-  // staging plan: one thread per row (j', k')
-  if (tid == 0) st_total = 0;
-  __syncthreads();
-  if (tid < STAGE_ROWS) {
-    int jj = j0 - STAGE_R + tid % (2 * STAGE_R + 1);
-    int kk = k0 - STAGE_R + tid / (2 * STAGE_R + 1);
-    int cnt = 0;
-    if (jj >= 0 && jj < dim && kk >= 0 && kk < dim) {
-      int c0 = xa + dim * (jj + dim * kk);
-      int base = cell_start[c0];
-      for (int x = 0; x <= xb - xa + 1; ++x) st_cell[tid][x] = cell_start[c0 + x] - base;
-      cnt = st_cell[tid][xb - xa + 1];
-    }
-    st_row_off[tid] = cnt;  // count for now
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int acc = 0;
-    for (int r = 0; r < STAGE_ROWS; ++r) {
-      int c = st_row_off[r];
-      st_row_off[r] = acc;
-      acc += c;
-    }
-    st_row_off[STAGE_ROWS] = acc;
-    st_total = acc;
-  }
-  __syncthreads();
-  const bool staged = st_total <= STAGE_CAP;
-  if (staged) {
-    for (int r = 0; r < STAGE_ROWS; ++r) {
-      int jj = j0 - STAGE_R + r % (2 * STAGE_R + 1);
-      int kk = k0 - STAGE_R + r / (2 * STAGE_R + 1);
-      if (jj < 0 || jj >= dim || kk < 0 || kk >= dim) continue;
-      int base = cell_start[xa + dim * (jj + dim * kk)];
-      int len = st_row_off[r + 1] - st_row_off[r];
-      for (int x = tid; x < len; x += KNN_THREADS) st_pts[st_row_off[r] + x] = sites[base + x];
-    }
-  }
-  __syncthreads();
-
-  KnnHeap H;
-  H.h = heap_base + tid;
-  H.K = K;
-  for (int qi = qb + tid; qi < qe; qi += KNN_THREADS) {
+  for (int q = blockIdx.x * KNN_WARPS + wib; q < n_query; q += gridDim.x * KNN_WARPS) {
     float4 Q;
-    int self = -1, orow = qi;
+    int self = -1, orow = q;
     if (CENTROIDS) {
       // centroid summed a, b, c, d from zero, then scaled (voronoi.cu:765-774)
-      orow = q_order[qi];
-      int4 t = tets[orow];
-      float4 a = verts[t.x], b = verts[t.y], c = verts[t.z], d = verts[t.w];
+      orow = q_order[q];
+      const int4 t = tets[orow];
+      const float4 a = verts[t.x], b = verts[t.y], c = verts[t.z], d = verts[t.w];
       Q.x = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), d.x), 0.25f);
       Q.y = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), d.y), 0.25f);
       Q.z = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), d.z), 0.25f);
       Q.w = 0.f;
     } else {
-      Q = sites[qi];
-      self = qi;
+      Q = sites[q];
+      self = q;
     }
-    const int ci = grid_axis(Q.x, dim), cj = j0, ck = k0;
-    H.cnt = 0;
-    H.root = ~0ull;
-    int r_next = 0;
-    if (staged) {
-      // own cell first, then the rest of the staged (2R+1)^3 block
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int r = 0; r < STAGE_ROWS; ++r) {
-          int dj = r % (2 * STAGE_R + 1) - STAGE_R, dk = r / (2 * STAGE_R + 1) - STAGE_R;
-          int jj = cj + dj, kk = ck + dk;
-          if (jj < 0 || jj >= dim || kk < 0 || kk >= dim) continue;
-          if (pass == 0 && (dj != 0 || dk != 0)) continue;
-          for (int ii = max(0, ci - STAGE_R); ii <= min(dim - 1, ci + STAGE_R); ++ii) {
-            bool own = (ii == ci && dj == 0 && dk == 0);
-            if (own != (pass == 0)) continue;
-            if (H.cnt == H.K && box_d2(Q, ii, jj, kk, dim, h) > __uint_as_float((unsigned)(H.root >> 32)))
-              continue;
-            int x = ii - xa;
-            int b = st_row_off[r] + st_cell[r][x], e = st_row_off[r] + st_cell[r][x + 1];
-            int gbase = cell_start[xa + dim * (jj + dim * kk)] - st_row_off[r];
-            for (int p = b; p < e; ++p) {
-              if (p + gbase == self) continue;
-              float4 P = st_pts[p];
-              H.push(heap_key(dist2(Q, P), P));
+    const int ci = grid_axis(Q.x, dim), cj = grid_axis(Q.y, dim), ck = grid_axis(Q.z, dim);
+    u64 L[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) L[s] = KEY_NONE;
+    u64 tau = KEY_NONE;  // current k-th key
+    int cnt = 0;         // buffered keys (warp-uniform)
+    for (int w = 0;; ++w) {
+      if (w > 0) {
+        if (ci - w < 0 && ci + w > dim - 1 && cj - w < 0 && cj + w > dim - 1 && ck - w < 0 && ck + w > dim - 1)
+          break;  // no cell left
+        if (tau != KEY_NONE) {
+          float lb = ring_bound(Q, ci, cj, ck, w, dim, h);
+          if (lb == FLT_MAX) break;
+          lb -= KNN_MARGIN;
+          if (lb > 0.f && __uint_as_float((unsigned)(tau >> 32)) < lb * lb) break;
+        }
+      }
+      const int ncell = w == 0 ? 1 : (2 * w + 1) * (2 * w + 1) * (2 * w + 1) - (2 * w - 1) * (2 * w - 1) * (2 * w - 1);
+      for (int cb = 0; cb < ncell; cb += 32) {
+        // one cell per lane: its site range, unless it is out of the grid
+        // or farther than the current k-th distance
+        int start = 0, count = 0;
+        const int t = cb + lane;
+        if (t < ncell) {
+          int di = 0, dj = 0, dk = 0;
+          if (w > 0) shell_cell(w, t, di, dj, dk);
+          const int i = ci + di, j = cj + dj, k = ck + dk;
+          if (i >= 0 && i < dim && j >= 0 && j < dim && k >= 0 && k < dim &&
+              (tau == KEY_NONE || box_d2(Q, i, j, k, dim, h) <= __uint_as_float((unsigned)(tau >> 32)))) {
+            const int c = i + dim * (j + dim * k);
+            start = cell_start[c];
+            count = cell_start[c + 1] - start;
+          }
+        }
+        int incl = count;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(KFULL, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(KFULL, incl, 31);
+        for (int f0 = 0; f0 < total; f0 += 32) {
+          const int f = f0 + lane;
+          // the lane (cell) holding flat index f: first lane with incl > f
+          int lo = 0;
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const int v = __shfl_sync(KFULL, incl, lo + step - 1);
+            if (v <= f) lo += step;
+          }
+          const int cstart = __shfl_sync(KFULL, start, lo);
+          const int cexcl = __shfl_sync(KFULL, incl - count, lo);
+          u64 key = KEY_NONE;
+          if (f < total) {
+            const int p = cstart + (f - cexcl);
+            if (p != self) {
+              const float4 P = sites[p];
+              key = heap_key(dist2(Q, P), P);
             }
+          }
+          const bool pass = key < tau;
+          const unsigned pm = __ballot_sync(KFULL, pass);
+          if (pass) buf[cnt + __popc(pm & lt_mask)] = key;
+          cnt += __popc(pm);
+          if (cnt >= 32) {
+            __syncwarp();
+            const u64 b = buf[lane];
+            const u64 rest = lane + 32 < cnt ? buf[lane + 32] : KEY_NONE;
+            __syncwarp();
+            if (lane + 32 < cnt) buf[lane] = rest;
+            cnt -= 32;
+            warp_merge<S>(L, b, lane);
+            tau = kth_key<S>(L, K);
+            __syncwarp();
           }
         }
       }
-      r_next = STAGE_R + 1;
+      if (cnt > 0) {
+        __syncwarp();
+        const u64 b = lane < cnt ? buf[lane] : KEY_NONE;
+        cnt = 0;
+        warp_merge<S>(L, b, lane);
+        tau = kth_key<S>(L, K);
+        __syncwarp();
+      }
     }
-    ring_walk(H, Q, self, ci, cj, ck, r_next, sites, cell_start, dim, h);
-    H.sort();
     unsigned* orow_ptr = out + (size_t)orow * K;
-    for (int j = 0; j < K; ++j)
-      orow_ptr[j] = j < H.cnt ? (unsigned)pos_of_id[(unsigned)(H.at(j) & 0xffffffffu)] : 0xffffffffu;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int e = s * 32 + lane;
+      if (e < K)
+        orow_ptr[e] = L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[(unsigned)(L[s] & 0xffffffffu)];
+    }
   }
 }
 
@@ -302,35 +282,55 @@ __global__ void k_pos_of_id(const float4* __restrict__ sites, int n, int* __rest
   pos_of_id[site_id(sites[i])] = i;
 }
 
-static size_t knn_smem_bytes(int k) { return sizeof(float4) * STAGE_CAP + sizeof(u64) * (size_t)k * KNN_THREADS; }
+static int g_knn_blocks = 0;  // resident CTAs x waves, set by knn_prepare
 
 int knn_prepare() {
-  const int smem = (int)knn_smem_bytes(MAX_SITE_K > MAX_TET_K ? MAX_SITE_K : MAX_TET_K);
-  VGB_CUDA_TRY(cudaFuncSetAttribute(k_knn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  VGB_CUDA_TRY(cudaFuncSetAttribute(k_knn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int dev = 0, sms = 0, per_sm = 0;
+  VGB_CUDA_TRY(cudaGetDevice(&dev));
+  VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn<2, false>, KNN_WARPS * 32, 0));
+  g_knn_blocks = sms * (per_sm > 0 ? per_sm : 1) * 8;
   return 0;
 }
 
-static int knn_blocks(int dim) { return dim * dim * ((dim + SEG_W - 1) / SEG_W); }
+template <bool CENTROIDS>
+static int launch_knn(const float4* sites, int n, int dim, const int* cell_start, int k, const float4* verts,
+                      const int4* tets, const int* q_order, int n_query, const int* pos_of_id, unsigned* out,
+                      cudaStream_t st) {
+  if (k < 1 || k > 128) {
+    set_error("kNN: k=%d outside [1, 128]", k);
+    return -1;
+  }
+  if (g_knn_blocks == 0 && knn_prepare()) return -1;
+  const int need = (n_query + KNN_WARPS - 1) / KNN_WARPS;
+  const int blocks = need < g_knn_blocks ? need : g_knn_blocks;
+  if (k <= 32)
+    k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
+                                                           n_query, pos_of_id, out);
+  else if (k <= 64)
+    k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
+                                                           n_query, pos_of_id, out);
+  else
+    k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
+                                                           n_query, pos_of_id, out);
+  VGB_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
 
 int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, int* pos_of_id, unsigned* out,
               cudaStream_t st) {
   if (n <= 0) return 0;
   k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, pos_of_id);
-  k_knn<false><<<knn_blocks(dim), KNN_THREADS, knn_smem_bytes(k), st>>>(sites, n, dim, cell_start, k, nullptr,
-                                                                        nullptr, nullptr, nullptr, pos_of_id, out);
   VGB_CUDA_TRY(cudaGetLastError());
-  return 0;
+  return launch_knn<false>(sites, n, dim, cell_start, k, nullptr, nullptr, nullptr, n, pos_of_id, out, st);
 }
 
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, cudaStream_t st) {
+  (void)tet_cell_start;
   if (n_tet <= 0) return 0;
-  k_knn<true><<<knn_blocks(dim), KNN_THREADS, knn_smem_bytes(k), st>>>(sites, n, dim, cell_start, k, verts, tets,
-                                                                       tet_order, tet_cell_start, pos_of_id, out);
-  VGB_CUDA_TRY(cudaGetLastError());
-  return 0;
+  return launch_knn<true>(sites, n, dim, cell_start, k, verts, tets, tet_order, n_tet, pos_of_id, out, st);
 }
 
 // ---------------------------------------------------------------------------
