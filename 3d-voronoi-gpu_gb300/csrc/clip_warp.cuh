@@ -125,6 +125,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
     int off = 0;
 #pragma unroll
     for (int k = 0; k < TRI_SLOTS; ++k) {
+      if (!m[k]) continue;
       if (m[k] & lane_bit) conf[off + __popc(m[k] & lt_mask)] = c.tri[k];
       off += __popc(m[k]);
     }
@@ -202,6 +203,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
   bool nonfinite = false;
 #pragma unroll
   for (int k = 0; k < TRI_SLOTS; ++k) {
+    if (c.vm[k] == 0u && base >= nb) continue;  // empty slot, nothing left to place
     const unsigned keep = c.vm[k] & ~m[k];
     const unsigned freem = ~keep;
     const int r = base + __popc(freem & lt_mask);

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
     for (int s = 0; s < S; ++s) L[s] = KEY_NONE;
     u64 tau = KEY_NONE;  // current k-th key
     int cnt = 0;         // buffered keys (warp-uniform)
+    int filled = 0;      // keys merged into the list so far
     for (int w = 0;; ++w) {
       if (w > 0) {
         if (ci - w < 0 && ci + w > dim - 1 && cj - w < 0 && cj + w > dim - 1 && ck - w < 0 && ck + w > dim - 1)
@@ -250,20 +251,29 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
             __syncwarp();
             if (lane + 32 < cnt) buf[lane] = rest;
             cnt -= 32;
+            filled += 32;
             warp_merge<S>(L, b, lane);
             tau = kth_key<S>(L, K);
             __syncwarp();
           }
         }
       }
-      if (cnt > 0) {
+      // flush once the list can hold K keys (the stop test needs the k-th)
+      if (cnt > 0 && filled + cnt >= K) {
         __syncwarp();
         const u64 b = lane < cnt ? buf[lane] : KEY_NONE;
+        filled += cnt;
         cnt = 0;
         warp_merge<S>(L, b, lane);
         tau = kth_key<S>(L, K);
         __syncwarp();
       }
+    }
+    if (cnt > 0) {
+      __syncwarp();
+      const u64 b = lane < cnt ? buf[lane] : KEY_NONE;
+      warp_merge<S>(L, b, lane);
+      __syncwarp();
     }
     unsigned* orow_ptr = out + (size_t)orow * K;
 #pragma unroll
