@@ -164,11 +164,13 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
         int es = e % 3;
         ea = tri_at(T, es);
         eb = tri_at(T, es == 2 ? 0 : es + 1);
+        // the twin (eb -> ea) as a directed-edge code lo | hi << 8; the
+        // codes of U = (u0, u1, u2) are its bytes 0-1, 1-2 and 2-0
+        const unsigned tw = eb | (ea << 8);
         bool twin = false;
         for (int q = 0; q < R; ++q) {
-          unsigned U = conf[q];
-          unsigned u0 = tri_at(U, 0), u1 = tri_at(U, 1), u2 = tri_at(U, 2);
-          twin |= (u0 == eb && u1 == ea) || (u1 == eb && u2 == ea) || (u2 == eb && u0 == ea);
+          const unsigned U = conf[q];
+          twin |= ((U & 0xffffu) == tw) | (((U >> 8) & 0xffffu) == tw) | (__byte_perm(U, 0u, 0x4402u) == tw);
         }
         isb = !twin;
       }
@@ -180,7 +182,15 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
       nb += __popc(bm);
     }
     __syncwarp();
-    if (nb <= MAX_TRI) {
+    if (nb <= WARP) {
+      // each boundary vertex starts exactly one edge and ends exactly one
+      const bool live = lane < nb;
+      const unsigned E = live ? bedge[lane] : 0u;
+      const unsigned ka = live ? (E & 0xffu) : (0x20000u | lane), kb = live ? (E >> 8) : (0x30000u | lane);
+      const unsigned ga = __match_any_sync(FULL, ka);
+      const unsigned gb = __match_any_sync(FULL, kb);
+      bad = live && (__popc(ga) != 1 || __popc(gb) != 1);
+    } else if (nb <= MAX_TRI) {
       for (int e = lane; e < nb; e += WARP) {
         unsigned E = bedge[e];
         int starts = 0, ends = 0;
