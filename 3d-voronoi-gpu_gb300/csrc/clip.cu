@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, int K,
     const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
     const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
-    const unsigned char* __restrict__ field, int fdim, const int* __restrict__ tet_order,
+    const unsigned char* __restrict__ field, const unsigned* __restrict__ field_sat, int fdim,
+    const int* __restrict__ tet_order,
     const int* __restrict__ tet_cell_start, int dim, float rt_max, const float4* __restrict__ tet_sph,
     const float* __restrict__ reach, const unsigned* __restrict__ reach_max_bits) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
@@ -342,14 +343,21 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         Rc = sqrtf(c.r2);
         // A cell that provably lies inside the mesh is its own clipped cell:
         // the sum over the tets it meets of (cell ^ tet) is the cell itself.
-        // field[f] = d > 0 marks an inside cell of the field grid whose
-        // points are at least (d - 1) * h from the mesh boundary; the cell
-        // lies within Rc of its site.
-        if (field && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f && seed.y <= 1000.f &&
-            seed.z >= 0.f && seed.z <= 1000.f) {
-          const int fd = field[grid_cell(seed.x, seed.y, seed.z, fdim)];
-          const float fh = 1000.f / (float)fdim;
-          interior = fd >= 2 && (float)(fd - 1) * fh > Rc * 1.001f + 0.01f;
+        // The cell lies within Rc of its site; when the box of field cells
+        // covering that ball holds no cell touched by the mesh boundary and
+        // the site's field cell is inside, the ball is inside the mesh.
+        const float Rq = Rc * 1.001f + 0.01f;
+        if (field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
+            seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f &&
+            field[grid_cell(seed.x, seed.y, seed.z, fdim)]) {
+          const int a0 = grid_axis(seed.x - Rq, fdim), a1 = grid_axis(seed.x + Rq, fdim) + 1;
+          const int b0 = grid_axis(seed.y - Rq, fdim), b1 = grid_axis(seed.y + Rq, fdim) + 1;
+          const int c0 = grid_axis(seed.z - Rq, fdim), c1 = grid_axis(seed.z + Rq, fdim) + 1;
+          const size_t W = (size_t)fdim + 1;
+          auto at = [&](int i, int j, int k) { return __ldg(field_sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
+          const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
+                                   at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
+          interior = touched == 0u;
         }
         take = interior;
         if (!interior) {
@@ -438,7 +446,8 @@ int clip_prepare() {
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
+                    unsigned long long* stats, const unsigned char* field, const unsigned* field_sat, int fdim,
+                    const int* tet_order,
                     const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st) {
   if (n <= 0) return 0;
@@ -449,11 +458,13 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   int blocks = (int)(want < need ? want : need);
   if (cell_tet)
     k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                            mom, stats, field, fdim, tet_order, tet_cell_start, dim,
+                                                            mom, stats, field, field_sat, fdim, tet_order,
+                                                            tet_cell_start, dim,
                                                             rt_max, tet_sph, reach, reach_max_bits);
   else
     k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                             mom, stats, nullptr, 0, nullptr, nullptr, 0, 0.f, nullptr,
+                                                             mom, stats, nullptr, nullptr, 0, nullptr, nullptr, 0, 0.f,
+                                                             nullptr,
                                                              nullptr, nullptr);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;

@@ -50,7 +50,8 @@ struct vgb_engine {
   float4* mom_f = nullptr;
   float* io_stage = nullptr;  // n x 3 floats for host-buffer steps
   unsigned long long* stats = nullptr;
-  unsigned char* field = nullptr;  // exact form: inside field of the mesh (else null)
+  unsigned char* field = nullptr;  // exact form: inside flags of the field grid (else null)
+  unsigned* field_sat = nullptr;   // exact form: summed touched counts of the field grid
   int fdim = 0;
   float rt_max = 0.f;              // exact form: largest tet corner distance from its centroid
   float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
@@ -161,7 +162,7 @@ void free_engine(vgb_engine* e) {
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
-                  e->io_stage, e->stats, e->field, e->reach, e->reach_max, e->tet_sph};
+                  e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -198,7 +199,7 @@ int run_pass(vgb_engine* e, int update) {
   MARK(4);
   if (e->cfg.method != VGB_METHOD_PLAIN) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
-                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->fdim,
+                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat, e->fdim,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->dim, e->rt_max,
                         e->tet_sph, e->reach, e->reach_max, st))
       return VGB_ERR_CUDA;
@@ -369,11 +370,8 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
   if (ce != cudaSuccess) { set_error("mesh upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   if (cfg.method == VGB_METHOD_CELL_TET && cfg.exact) {
-    // field grid twice as fine as the site grid, at most 512 per side
-    e->fdim = std::min(512, std::max(8, 2 * e->dim));
-    std::vector<unsigned char> field;
-    build_inside_field(verts, n_vert, tets, n_tet, e->fdim, field);
     float rt = 0.f;
+    double mesh_vol = 0.0;
     for (int t = 0; t < n_tet; ++t) {
       const float* p[4];
       float c[3] = {0.f, 0.f, 0.f};
@@ -385,15 +383,33 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
         float dx = p[q][0] - c[0], dy = p[q][1] - c[1], dz = p[q][2] - c[2];
         rt = std::max(rt, std::sqrt(dx * dx + dy * dy + dz * dz));
       }
+      double a[3], b[3], d3[3];
+      for (int d = 0; d < 3; ++d) {
+        a[d] = (double)p[1][d] - p[0][d];
+        b[d] = (double)p[2][d] - p[0][d];
+        d3[d] = (double)p[3][d] - p[0][d];
+      }
+      mesh_vol += std::fabs(a[0] * (b[1] * d3[2] - b[2] * d3[1]) + a[1] * (b[2] * d3[0] - b[0] * d3[2]) +
+                            a[2] * (b[0] * d3[1] - b[1] * d3[0])) / 6.0;
     }
     e->rt_max = rt * 1.001f + 1e-3f;
-    if ((rc = dalloc(&e->field, field.size())) || (rc = dalloc(&e->reach, n_tet)) ||
+    // field cells about a third of the site spacing in the mesh, at most
+    // 512 per side
+    const double spacing = std::cbrt(std::max(mesh_vol, 1.0) / std::max(n_site, 1));
+    e->fdim = (int)std::min(512.0, std::max(8.0, std::ceil(3000.0 / spacing)));
+    std::vector<unsigned char> field;
+    std::vector<unsigned> field_sat;
+    build_inside_field(verts, n_vert, tets, n_tet, e->fdim, field, field_sat);
+    if ((rc = dalloc(&e->field, field.size())) || (rc = dalloc(&e->field_sat, field_sat.size())) ||
+        (rc = dalloc(&e->reach, n_tet)) ||
         (rc = dalloc(&e->reach_max, 1)) || (rc = dalloc(&e->tet_sph, n_tet))) {
       free_engine(e);
       return rc;
     }
     if (tet_spheres(e->verts, e->tets, e->tet_order, n_tet, e->tet_sph, e->st)) { free_engine(e); return VGB_ERR_CUDA; }
     ce = cudaMemcpy(e->field, field.data(), field.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(e->field_sat, field_sat.data(), sizeof(unsigned) * field_sat.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   }
   if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }

@@ -1,19 +1,21 @@
 // Inside field of a tet mesh (host, once per mesh): which grid cells lie
-// inside the mesh, and how far each is from the mesh boundary.
+// inside the mesh, and which may meet its boundary.
 //
-// A grid of bdim^3 cells over [0,1000]^3 (the path's coordinate frame):
+// A grid of dim^3 cells over [0,1000]^3 (the path's coordinate frame):
 //   1. boundary faces = tet faces used by exactly one tet (faces bucketed by
 //      their smallest vertex, then matched inside the bucket);
 //   2. every grid cell overlapped by a boundary face's bounding box (plus a
-//      margin) is a boundary cell;
-//   3. a multi-source BFS over the 26-neighbourhood gives each cell its
-//      Chebyshev distance d, in cells, to the nearest boundary cell, so every
-//      point of the cell is at least (d - 1) * h from the mesh boundary;
-//   4. a cell with d >= 1 that holds a tet centroid lies inside the mesh (it
-//      meets the mesh and does not meet its boundary).
-// field[c] = d (capped at 255) for inside cells, 0 otherwise.  A convex
-// region of points within (field[c] - 1) * h of a point of cell c is then
-// inside the mesh.
+//      margin) is touched: the boundary surface meets no untouched cell;
+//   3. the untouched cells split into face-connected regions, each wholly
+//      inside or wholly outside the mesh (a face-adjacent step between two
+//      untouched cells cannot cross the boundary surface); a region holding a
+//      tet centroid is inside;
+//   4. a summed-volume table of the touched cells answers "does this box of
+//      cells meet the boundary" with eight reads.
+// inside[c] = 1 for inside cells; sat has (dim+1)^3 entries, sat(i,j,k) =
+// number of touched cells in [0,i) x [0,j) x [0,k).  A convex region whose
+// box of cells holds no touched cell and contains an inside cell lies inside
+// the mesh.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -28,9 +30,11 @@ static inline int axis_cell(float p, int dim) {
 }
 
 int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim,
-                       std::vector<unsigned char>& field) {
+                       std::vector<unsigned char>& inside, std::vector<unsigned>& sat) {
   const long long nc = (long long)dim * dim * dim;
-  field.assign((size_t)nc, 0);
+  const size_t W = (size_t)dim + 1;
+  inside.assign((size_t)nc, 0);
+  sat.assign(W * W * W, 0u);
   if (nt <= 0 || nv <= 0) return 0;
   // 1. boundary faces
   std::vector<int> count((size_t)nv + 1, 0);
@@ -77,41 +81,49 @@ int build_inside_field(const float* verts, int nv, const int* tets, int nt, int 
       it = jt;
     }
   }
-  // 3. Chebyshev distance to the boundary cells
-  std::vector<unsigned char> dist((size_t)nc, 255);
-  std::vector<int> frontier, next;
-  for (long long c = 0; c < nc; ++c)
-    if (touch[(size_t)c]) {
-      dist[(size_t)c] = 0;
-      frontier.push_back((int)c);
-    }
-  for (int d = 1; d < 255 && !frontier.empty(); ++d) {
-    next.clear();
-    for (int c : frontier) {
-      int i = c % dim, j = (c / dim) % dim, k = c / (dim * dim);
-      for (int dk = -1; dk <= 1; ++dk)
-        for (int dj = -1; dj <= 1; ++dj)
-          for (int di = -1; di <= 1; ++di) {
-            int ii = i + di, jj = j + dj, kk = k + dk;
-            if (ii < 0 || jj < 0 || kk < 0 || ii >= dim || jj >= dim || kk >= dim) continue;
-            size_t n = (size_t)ii + (size_t)dim * (jj + (size_t)dim * kk);
-            if (dist[n] == 255) {
-              dist[n] = (unsigned char)d;
-              next.push_back((int)n);
-            }
-          }
-    }
-    frontier.swap(next);
-  }
-  // 4. inside cells: away from the boundary and holding a tet centroid
+  // 3. inside regions: flood the untouched cells face to face from every
+  //    untouched cell holding a tet centroid
+  std::vector<int> stack;
   for (int t = 0; t < nt; ++t) {
     float c[3] = {0.f, 0.f, 0.f};
     for (int q = 0; q < 4; ++q)
       for (int d = 0; d < 3; ++d) c[d] += verts[3 * (size_t)tets[4 * (size_t)t + q] + d];
     int i = axis_cell(c[0] * 0.25f, dim), j = axis_cell(c[1] * 0.25f, dim), k = axis_cell(c[2] * 0.25f, dim);
     size_t cc = (size_t)i + (size_t)dim * (j + (size_t)dim * k);
-    if (dist[cc] >= 1) field[cc] = dist[cc];
+    if (touch[cc] || inside[cc]) continue;
+    inside[cc] = 1;
+    stack.push_back((int)cc);
+    while (!stack.empty()) {
+      const int c0 = stack.back();
+      stack.pop_back();
+      const int ci = c0 % dim, cj = (c0 / dim) % dim, ck = c0 / (dim * dim);
+      const int nb[6][3] = {{ci - 1, cj, ck}, {ci + 1, cj, ck}, {ci, cj - 1, ck},
+                            {ci, cj + 1, ck}, {ci, cj, ck - 1}, {ci, cj, ck + 1}};
+      for (const auto& q : nb) {
+        if (q[0] < 0 || q[1] < 0 || q[2] < 0 || q[0] >= dim || q[1] >= dim || q[2] >= dim) continue;
+        const size_t n = (size_t)q[0] + (size_t)dim * (q[1] + (size_t)dim * q[2]);
+        if (!touch[n] && !inside[n]) {
+          inside[n] = 1;
+          stack.push_back((int)n);
+        }
+      }
+    }
   }
+  // 4. summed-volume table of the touched cells
+  for (int k = 0; k < dim; ++k)
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i)
+        sat[(size_t)(i + 1) + W * ((size_t)(j + 1) + W * (size_t)(k + 1))] =
+            touch[(size_t)i + (size_t)dim * (j + (size_t)dim * k)];
+  for (size_t k = 1; k < W; ++k)
+    for (size_t j = 1; j < W; ++j)
+      for (size_t i = 1; i < W; ++i) sat[i + W * (j + W * k)] += sat[(i - 1) + W * (j + W * k)];
+  for (size_t k = 1; k < W; ++k)
+    for (size_t j = 1; j < W; ++j)
+      for (size_t i = 1; i < W; ++i) sat[i + W * (j + W * k)] += sat[i + W * ((j - 1) + W * k)];
+  for (size_t k = 1; k < W; ++k)
+    for (size_t j = 1; j < W; ++j)
+      for (size_t i = 1; i < W; ++i) sat[i + W * (j + W * k)] += sat[i + W * (j + W * (k - 1))];
   return 0;
 }
 

@@ -142,14 +142,16 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 // Site-major clipping of every candidate pair -- the tet-cell method, or the
 // cell-tet method when cell_tet -- with per-site moments relative to the
 // site: mom[s] = (vol, mx, my, mz).
-// Exact form (cell-tet only; all of field, tet_order and tet_cell_start
-// given): cells inside the mesh (field: fdim^3 bytes from build_inside_field)
-// are taken whole, other cells are clipped by every tet whose centroid is
-// within Rc + rt_max (tets sorted by centroid cell of the site grid, dim^3
-// cells).  Otherwise the candidate lists site_start / site_tets are used.
+// Exact form (cell-tet only; all of field, field_sat, tet_order and
+// tet_cell_start given): cells inside the mesh (field: fdim^3 inside flags,
+// field_sat: (fdim+1)^3 summed touched counts, from build_inside_field) are
+// taken whole, other cells are clipped by every tet within reach (tets sorted
+// by centroid cell of the site grid, dim^3 cells).  Otherwise the candidate
+// lists site_start / site_tets are used.
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
                     const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, int fdim, const int* tet_order,
+                    unsigned long long* stats, const unsigned char* field, const unsigned* field_sat, int fdim,
+                    const int* tet_order,
                     const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st);
 
@@ -169,5 +171,6 @@ int clip_prepare();
 #include <vector>
 namespace vgb {
 // Inside field of a mesh on a dim^3 grid over [0,1000]^3 (mesh_field.cpp).
-int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim, std::vector<unsigned char>& field);
+int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim, std::vector<unsigned char>& inside,
+                       std::vector<unsigned>& sat);
 }  // namespace vgb
