@@ -350,8 +350,8 @@ def run_ours(args):
                   FLOPS_NEW_VERTEX * stats["new_vertices"] + FLOPS_FINAL_VERTEX * stats["final_vertices"])
     clip_tf = clip_flops / (phases["clip"] / 1e3) / 1e12
     kname = {"cell_tet": "k_clip_site<true>", "site_major": "k_clip_site<false>", "plain": "k_clip_plain"}[args.method]
-    ktraffic = profile_traffic({"cell_tet": "clip_cell_tet", "site_major": "clip_tet_cell",
-                                "plain": "clip_plain"}[args.method], args.workload)
+    ktraffic = profile_traffic("clip_exact" if exact else {"cell_tet": "clip_cell_tet", "site_major": "clip_tet_cell",
+                                                          "plain": "clip_plain"}[args.method], args.workload)
     roofline = {"kernel": kname,
                 "bound": "fp32", "achieved": round(clip_tf, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
                 "frac": round(clip_tf / fp32_peak, 4), "traffic": ktraffic,
