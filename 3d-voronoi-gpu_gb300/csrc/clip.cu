@@ -85,13 +85,13 @@ struct SiteSmem {
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
 template <bool CELL_TET>
 __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
-    const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, int K,
-    const float4* __restrict__ verts, const int4* __restrict__ tets, const int* __restrict__ site_start,
-    const int* __restrict__ site_tets, dmom4* __restrict__ mom, unsigned long long* __restrict__ stats,
-    const unsigned char* __restrict__ field, const unsigned* __restrict__ field_sat, int fdim,
-    const int* __restrict__ tet_order,
-    const int* __restrict__ tet_cell_start, int dim, float rt_max, const float4* __restrict__ tet_sph,
-    const float* __restrict__ reach, const unsigned* __restrict__ reach_max_bits) {
+    const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
+    const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
+    const int4* __restrict__ tets, const int* __restrict__ site_start, const int* __restrict__ site_tets,
+    dmom4* __restrict__ mom, unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
+    const unsigned* __restrict__ field_sat, const int* __restrict__ tet_order,
+    const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
+    const unsigned* __restrict__ reach_max_bits) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -103,10 +103,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
   __syncwarp();
 
   for (int s = blockIdx.x * CLIP_WARPS + wib; s < n; s += gridDim.x * CLIP_WARPS) {
+    int pidx;
+    const ProbDesc P = prob_for(probs, site_prob, s, lone, pidx);
+    const int K = P.K;
     const float4 seed = sites[s];
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
+    const unsigned* krow = knn + P.knn_off + (size_t)(s - P.site_off) * K;
     for (int j = lane; j < K; j += WARP) {
-      float4 B = sites[knn[(size_t)s * K + j]];
+      float4 B = sites[krow[j]];
       float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
       float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
       S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
           if (base >= se) {
             if (++seg >= nseg) break;
             if (exact) {
-              const int row = dim * ((j0 + seg % nj) + dim * (k0 + seg / nj));
+              const int row = P.cell_off + P.dim * ((j0 + seg % nj) + P.dim * (k0 + seg / nj));
               base = tet_cell_start[i0 + row];
               se = tet_cell_start[i1 + row + 1];
             } else {
@@ -347,14 +351,16 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         // covering that ball holds no cell touched by the mesh boundary and
         // the site's field cell is inside, the ball is inside the mesh.
         const float Rq = Rc * 1.001f + 0.01f;
+        const int fdim = P.fdim;
         if (field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
             seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f &&
-            field[grid_cell(seed.x, seed.y, seed.z, fdim)]) {
+            field[P.field_off + grid_cell(seed.x, seed.y, seed.z, fdim)]) {
           const int a0 = grid_axis(seed.x - Rq, fdim), a1 = grid_axis(seed.x + Rq, fdim) + 1;
           const int b0 = grid_axis(seed.y - Rq, fdim), b1 = grid_axis(seed.y + Rq, fdim) + 1;
           const int c0 = grid_axis(seed.z - Rq, fdim), c1 = grid_axis(seed.z + Rq, fdim) + 1;
           const size_t W = (size_t)fdim + 1;
-          auto at = [&](int i, int j, int k) { return __ldg(field_sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
+          const unsigned* sat = field_sat + P.sat_off;
+          auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
           const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
                                    at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
           interior = touched == 0u;
@@ -386,7 +392,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
           // centroid within Rc + rt_max of the site, and no tet reaches
           // farther than the largest reach
           if (exact) {
-            const float R = fminf(Rc + rt_max * 1.001f, __uint_as_float(*reach_max_bits)) + 0.01f;
+            const int dim = P.dim;
+            const float R = fminf(Rc + P.rt_max * 1.001f, __uint_as_float(reach_max_bits[pidx])) + 0.01f;
             i0 = grid_axis(seed.x - R, dim);
             i1 = grid_axis(seed.x + R, dim);
             j0 = grid_axis(seed.y - R, dim);
@@ -444,11 +451,11 @@ int clip_prepare() {
   return 0;
 }
 
-int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
-                    const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, const unsigned* field_sat, int fdim,
-                    const int* tet_order,
-                    const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
+int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
+                    const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
+                    const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
+                    const unsigned char* field, const unsigned* field_sat, const int* tet_order,
+                    const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
@@ -457,15 +464,14 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
   int blocks = (int)(want < need ? want : need);
   if (cell_tet)
-    k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                            mom, stats, field, field_sat, fdim, tet_order,
-                                                            tet_cell_start, dim,
-                                                            rt_max, tet_sph, reach, reach_max_bits);
+    k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
+                                                            site_start, site_tets, mom, stats, field, field_sat,
+                                                            tet_order, tet_cell_start, tet_sph, reach,
+                                                            reach_max_bits);
   else
-    k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, k, verts, tets, site_start, site_tets,
-                                                             mom, stats, nullptr, nullptr, 0, nullptr, nullptr, 0, 0.f,
-                                                             nullptr,
-                                                             nullptr, nullptr);
+    k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
+                                                             site_start, site_tets, mom, stats, nullptr, nullptr,
+                                                             nullptr, nullptr, nullptr, nullptr, nullptr);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -29,6 +29,7 @@ struct vgb_engine {
   vgb_config cfg;
   cudaStream_t st = nullptr;
   int n_vert = 0, n_tet = 0, n = 0, K = 0, tk = 0, dim = 0;
+  vgb::ProbDesc prob{};  // the engine's problem (a batch of one)
   long long ncell = 0;
   float4* verts = nullptr;
   int4* tets = nullptr;
@@ -175,14 +176,17 @@ int run_pass(vgb_engine* e, int update) {
 #define MARK(i) \
   if (e->timed) VGB_CUDA_TRY(cudaEventRecord(e->ev[i], st))
   MARK(0);
-  if (grid_sort(e->sites, e->sites_tmp, e->n, e->dim, e->cell_start, e->cell_fill, e->site_cell, e->scan_tmp, st))
+  if (grid_sort(e->sites, e->sites_tmp, e->n, e->ncell, nullptr, nullptr, e->prob, e->cell_start, e->cell_fill,
+                e->site_cell, e->scan_tmp, st))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(e->sites, e->sites_tmp, sizeof(float4) * e->n, cudaMemcpyDeviceToDevice, st));
   MARK(1);
-  if (knn_sites(e->sites, e->n, e->dim, e->cell_start, e->K, e->pos_of_id, e->knn, st)) return VGB_ERR_CUDA;
+  if (knn_sites(e->sites, e->n, e->cell_start, nullptr, nullptr, e->prob, e->K, e->pos_of_id, e->knn, st))
+    return VGB_ERR_CUDA;
   MARK(2);
   const bool exact = e->field != nullptr;
-  if (exact && tet_reach(e->sites, e->dim, e->cell_start, e->tet_sph, e->n_tet, e->reach, e->reach_max, st))
+  if (exact && tet_reach(e->sites, e->cell_start, nullptr, nullptr, e->prob, 1, e->tet_sph, e->n_tet, e->reach,
+                         e->reach_max, st))
     return VGB_ERR_CUDA;
   if (!exact &&
       knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
@@ -198,10 +202,10 @@ int run_pass(vgb_engine* e, int update) {
   if (e->cfg.method == VGB_METHOD_PLAIN) VGB_CUDA_TRY(cudaMemsetAsync(e->mom_f, 0, sizeof(float4) * e->n, st));
   MARK(4);
   if (e->cfg.method != VGB_METHOD_PLAIN) {
-    if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, e->K, e->verts, e->tets,
-                        e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat, e->fdim,
-                        exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->dim, e->rt_max,
-                        e->tet_sph, e->reach, e->reach_max, st))
+    if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
+                        e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
+                        exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
+                        e->reach_max, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -315,6 +319,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   e->dim = cfg.grid_dim > 0 ? cfg.grid_dim : vgb_grid_dim(n_site);
   e->ncell = (long long)e->dim * e->dim * e->dim;
   if (e->ncell >= (1LL << 31) - 1) { set_error("grid too large"); delete e; return VGB_ERR_INVALID; }
+  e->prob = lone_problem(n_site, e->dim, n_tet, e->K);
   cudaError_t ce = cudaSetDevice(cfg.device);
   if (ce != cudaSuccess) { set_error("cudaSetDevice(%d): %s", cfg.device, cudaGetErrorString(ce)); delete e; return VGB_ERR_CUDA; }
   if (knn_prepare() || clip_prepare()) { delete e; return VGB_ERR_CUDA; }
@@ -356,7 +361,8 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     // tets by centroid cell, once per mesh and grid
     int* tcell = nullptr;
     if (dalloc(&tcell, n_tet) != VGB_OK) { free_engine(e); return VGB_ERR_NOMEM; }
-    if (tets_by_cell(e->verts, e->tets, n_tet, e->dim, e->tet_cell_start, e->cell_fill, tcell, e->tet_order,
+    if (tets_by_cell(e->verts, e->tets, n_tet, e->ncell, nullptr, nullptr, e->prob, e->tet_cell_start, e->cell_fill,
+                     tcell, e->tet_order,
                      e->scan_tmp, e->st)) {
       cudaFree(tcell);
       free_engine(e);
@@ -393,6 +399,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
                             a[2] * (b[0] * d3[1] - b[1] * d3[0])) / 6.0;
     }
     e->rt_max = rt * 1.001f + 1e-3f;
+    e->prob.rt_max = e->rt_max;
     // field cells about a third of the site spacing in the mesh, at most
     // 512 per side
     const double spacing = std::cbrt(std::max(mesh_vol, 1.0) / std::max(n_site, 1));
@@ -400,6 +407,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     std::vector<unsigned char> field;
     std::vector<unsigned> field_sat;
     build_inside_field(verts, n_vert, tets, n_tet, e->fdim, field, field_sat);
+    e->prob.fdim = e->fdim;
     if ((rc = dalloc(&e->field, field.size())) || (rc = dalloc(&e->field_sat, field_sat.size())) ||
         (rc = dalloc(&e->reach, n_tet)) ||
         (rc = dalloc(&e->reach_max, 1)) || (rc = dalloc(&e->tet_sph, n_tet))) {

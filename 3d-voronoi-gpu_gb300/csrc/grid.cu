@@ -125,12 +125,15 @@ int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t 
 // ---------------------------------------------------------------------------
 // Grid sort.
 // ---------------------------------------------------------------------------
-__global__ void k_grid_count(const float4* __restrict__ in, int n, int dim, int* __restrict__ count,
+__global__ void k_grid_count(const float4* __restrict__ in, int n, const ProbDesc* __restrict__ probs,
+                             const int* __restrict__ site_prob, ProbDesc lone, int* __restrict__ count,
                              int* __restrict__ site_cell) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int pb;
+  const ProbDesc P = prob_for(probs, site_prob, i, lone, pb);
   float4 p = in[i];
-  int c = grid_cell(p.x, p.y, p.z, dim);
+  int c = P.cell_off + grid_cell(p.x, p.y, p.z, P.dim);
   site_cell[i] = c;
   atomicAdd(count + c, 1);
 }
@@ -166,13 +169,12 @@ __global__ void k_cell_order(float4* __restrict__ pts, const int* __restrict__ s
   }
 }
 
-int grid_sort(const float4* in, float4* out, int n, int dim, int* cell_start, int* cell_fill, int* site_cell,
-              int* scan_tmp, cudaStream_t st) {
-  long long ncell = (long long)dim * dim * dim;
+int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbDesc* probs, const int* site_prob,
+              const ProbDesc& lone, int* cell_start, int* cell_fill, int* site_cell, int* scan_tmp, cudaStream_t st) {
   VGB_CUDA_TRY(cudaMemsetAsync(cell_start, 0, sizeof(int) * (ncell + 1), st));
   VGB_CUDA_TRY(cudaMemsetAsync(cell_fill, 0, sizeof(int) * ncell, st));
   if (n > 0) {
-    k_grid_count<<<(n + 255) / 256, 256, 0, st>>>(in, n, dim, cell_start, site_cell);
+    k_grid_count<<<(n + 255) / 256, 256, 0, st>>>(in, n, probs, site_prob, lone, cell_start, site_cell);
     VGB_CUDA_TRY(cudaGetLastError());
   }
   if (scan_exclusive(cell_start, cell_start, ncell + 1, scan_tmp, st)) return -2;

@@ -114,7 +114,9 @@ int kn_prepare_ex(kn_problem** out, const float* xyz, int n, int k) {
     ce = cudaGetLastError();
   }
   if (ce != cudaSuccess) { set_error("kn_prepare upload: %s", cudaGetErrorString(ce)); cudaFree(stage); kn_release(kn); return VGB_ERR_CUDA; }
-  int rc = grid_sort(im->in, im->sorted, n, dim, im->cell_start, im->cell_fill, im->site_cell, im->scan_tmp, st);
+  const ProbDesc lone = lone_problem(n, dim, 0, k);
+  int rc = grid_sort(im->in, im->sorted, n, nc, nullptr, nullptr, lone, im->cell_start, im->cell_fill, im->site_cell,
+                     im->scan_tmp, st);
   if (!rc) {
     k_kn_views<<<(n + 255) / 256, 256, 0, st>>>(im->sorted, n, kn->d_stored_points, kn->d_permutation);
     k_kn_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(im->cell_start, (int)nc, kn->d_counters, kn->d_ptrs);
@@ -133,7 +135,9 @@ int kn_solve_ex(kn_problem* kn) {
   if (!kn || !kn->impl) { set_error("kn_solve: NULL problem"); return VGB_ERR_INVALID; }
   KnImpl* im = static_cast<KnImpl*>(kn->impl);
   if (knn_prepare()) return VGB_ERR_CUDA;
-  if (knn_sites(im->sorted, kn->allocated_points, kn->dimx, im->cell_start, kn->k, im->pos_of_id, kn->d_knearests, 0))
+  const ProbDesc lone = lone_problem(kn->allocated_points, kn->dimx, 0, kn->k);
+  if (knn_sites(im->sorted, kn->allocated_points, im->cell_start, nullptr, nullptr, lone, kn->k, im->pos_of_id,
+                kn->d_knearests, 0))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaStreamSynchronize(0));
   return VGB_OK;

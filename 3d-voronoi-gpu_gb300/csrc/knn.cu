@@ -151,9 +151,11 @@ __device__ __forceinline__ u64 kth_key(const u64 (&L)[S], int K) {
 }
 
 template <int S, bool CENTROIDS>
-__global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict__ sites, int n, int dim,
-                                                        const int* __restrict__ cell_start, int K,
-                                                        const float4* __restrict__ verts,
+__global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict__ sites,
+                                                        const int* __restrict__ cell_start,
+                                                        const ProbDesc* __restrict__ probs,
+                                                        const int* __restrict__ site_prob, ProbDesc lone,
+                                                        int kq, const float4* __restrict__ verts,
                                                         const int4* __restrict__ tets,
                                                         const int* __restrict__ q_order, int n_query,
                                                         const int* __restrict__ pos_of_id,
@@ -162,8 +164,13 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
-  const float h = 1000.f / (float)dim;
   for (int q = blockIdx.x * KNN_WARPS + wib; q < n_query; q += gridDim.x * KNN_WARPS) {
+    // centroid queries belong to the lone problem
+    int pq = 0;
+    const ProbDesc P = CENTROIDS ? lone : prob_for(probs, site_prob, q, lone, pq);
+    const int dim = P.dim, cbase = P.cell_off;
+    const int K = CENTROIDS ? kq : P.K;
+    const float h = 1000.f / (float)dim;
     float4 Q;
     int self = -1, orow = q;
     if (CENTROIDS) {
@@ -209,7 +216,7 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
           const int i = ci + di, j = cj + dj, k = ck + dk;
           if (i >= 0 && i < dim && j >= 0 && j < dim && k >= 0 && k < dim &&
               (tau == KEY_NONE || box_d2(Q, i, j, k, dim, h) <= __uint_as_float((unsigned)(tau >> 32)))) {
-            const int c = i + dim * (j + dim * k);
+            const int c = cbase + i + dim * (j + dim * k);
             start = cell_start[c];
             count = cell_start[c + 1] - start;
           }
@@ -275,21 +282,25 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
       warp_merge<S>(L, b, lane);
       __syncwarp();
     }
-    unsigned* orow_ptr = out + (size_t)orow * K;
+    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * K : out + P.knn_off + (size_t)(q - P.site_off) * K;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int e = s * 32 + lane;
       if (e < K)
-        orow_ptr[e] = L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[(unsigned)(L[s] & 0xffffffffu)];
+        orow_ptr[e] =
+            L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[P.site_off + (int)(L[s] & 0xffffffffu)];
     }
   }
 }
 
-// pos_of_id[id] = sorted position of the site with that id.
-__global__ void k_pos_of_id(const float4* __restrict__ sites, int n, int* __restrict__ pos_of_id) {
+// pos_of_id[site_off + id] = sorted position of the site with that id.
+__global__ void k_pos_of_id(const float4* __restrict__ sites, int n, const ProbDesc* __restrict__ probs,
+                            const int* __restrict__ site_prob, ProbDesc lone, int* __restrict__ pos_of_id) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  pos_of_id[site_id(sites[i])] = i;
+  int p;
+  const ProbDesc P = prob_for(probs, site_prob, i, lone, p);
+  pos_of_id[P.site_off + site_id(sites[i])] = i;
 }
 
 static int g_knn_blocks = 0;  // resident CTAs x waves, set by knn_prepare
@@ -304,35 +315,36 @@ int knn_prepare() {
 }
 
 template <bool CENTROIDS>
-static int launch_knn(const float4* sites, int n, int dim, const int* cell_start, int k, const float4* verts,
-                      const int4* tets, const int* q_order, int n_query, const int* pos_of_id, unsigned* out,
-                      cudaStream_t st) {
-  if (k < 1 || k > 128) {
-    set_error("kNN: k=%d outside [1, 128]", k);
+static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* site_prob,
+                      const ProbDesc& lone, int kmax, int kq, const float4* verts, const int4* tets,
+                      const int* q_order, int n_query, const int* pos_of_id, unsigned* out, cudaStream_t st) {
+  if (kmax < 1 || kmax > 128) {
+    set_error("kNN: k=%d outside [1, 128]", kmax);
     return -1;
   }
   if (g_knn_blocks == 0 && knn_prepare()) return -1;
   const int need = (n_query + KNN_WARPS - 1) / KNN_WARPS;
   const int blocks = need < g_knn_blocks ? need : g_knn_blocks;
-  if (k <= 32)
-    k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
-                                                           n_query, pos_of_id, out);
-  else if (k <= 64)
-    k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
-                                                           n_query, pos_of_id, out);
+  if (kmax <= 32)
+    k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
+                                                           tets, q_order, n_query, pos_of_id, out);
+  else if (kmax <= 64)
+    k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
+                                                           tets, q_order, n_query, pos_of_id, out);
   else
-    k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, n, dim, cell_start, k, verts, tets, q_order,
-                                                           n_query, pos_of_id, out);
+    k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
+                                                           tets, q_order, n_query, pos_of_id, out);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
-int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, int* pos_of_id, unsigned* out,
-              cudaStream_t st) {
+int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, cudaStream_t st) {
   if (n <= 0) return 0;
-  k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, pos_of_id);
+  k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, probs, site_prob, lone, pos_of_id);
   VGB_CUDA_TRY(cudaGetLastError());
-  return launch_knn<false>(sites, n, dim, cell_start, k, nullptr, nullptr, nullptr, n, pos_of_id, out, st);
+  return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kmax, 0, nullptr, nullptr, nullptr, n,
+                           pos_of_id, out, st);
 }
 
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
@@ -340,7 +352,9 @@ int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start
                       int n_tet, int k, unsigned* out, cudaStream_t st) {
   (void)tet_cell_start;
   if (n_tet <= 0) return 0;
-  return launch_knn<true>(sites, n, dim, cell_start, k, verts, tets, tet_order, n_tet, pos_of_id, out, st);
+  const ProbDesc lone = lone_problem(n, dim, n_tet, k);
+  return launch_knn<true>(sites, cell_start, nullptr, nullptr, lone, k, k, verts, tets, tet_order, n_tet, pos_of_id,
+                          out, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -352,12 +366,16 @@ int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start
 // reach bounds every cell's search radius.  Thread per tet, in centroid-cell
 // order; a ring walk keeps the single nearest site.
 // ---------------------------------------------------------------------------
-__global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int* __restrict__ cell_start,
+__global__ void k_tet_reach(const float4* __restrict__ sites, const int* __restrict__ cell_start,
+                            const ProbDesc* __restrict__ probs, const int* __restrict__ tet_prob, ProbDesc lone,
                             const float4* __restrict__ tet_sph, int n_tet, float* __restrict__ reach,
                             unsigned* __restrict__ reach_max_bits) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   float rr = 0.f;
+  int pq = 0;
   if (q < n_tet) {
+    const ProbDesc P = prob_for(probs, tet_prob, q, lone, pq);
+    const int dim = P.dim, cbase = P.cell_off;
     const float4 sp = tet_sph[q];
     const float4 Q = make_float4(sp.x, sp.y, sp.z, 0.f);
     const float h = 1000.f / (float)dim;
@@ -384,7 +402,7 @@ __global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int
             const int i = ci + di;
             if (i < 0 || i >= dim) continue;
             if (best < FLT_MAX && box_d2(Q, i, j, k, dim, h) > best) continue;
-            const int cc = i + dim * (j + dim * k);
+            const int cc = cbase + i + dim * (j + dim * k);
             for (int p = cell_start[cc]; p < cell_start[cc + 1]; ++p) best = fminf(best, dist2(Q, sites[p]));
           }
         }
@@ -393,24 +411,26 @@ __global__ void k_tet_reach(const float4* __restrict__ sites, int dim, const int
     rr = (sqrtf(best) + 2.f * sp.w) * 1.0001f + 1e-3f;
     reach[q] = rr;
   }
-  // block max, then one atomic per block (non-negative floats order as ints)
-  __shared__ float bmax[8];
-  float m = rr;
+  // per-problem max: one atomic per warp when the warp holds one problem
+  // (non-negative floats order as ints; lanes past the end hold 0)
+  const int p0 = __shfl_sync(0xffffffffu, pq, 0);
+  if (__all_sync(0xffffffffu, q >= n_tet || pq == p0)) {
+    float m = rr;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) bmax[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, bmax[w]);
-    atomicMax(reach_max_bits, __float_as_uint(m));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reach_max_bits + p0, __float_as_uint(m));
+  } else if (q < n_tet) {
+    atomicMax(reach_max_bits + pq, __float_as_uint(rr));
   }
 }
 
-int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* tet_sph, int n_tet, float* reach,
+int tet_reach(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* tet_prob,
+              const ProbDesc& lone, int n_prob, const float4* tet_sph, int n_tet, float* reach,
               unsigned* reach_max_bits, cudaStream_t st) {
-  VGB_CUDA_TRY(cudaMemsetAsync(reach_max_bits, 0, sizeof(unsigned), st));
+  VGB_CUDA_TRY(cudaMemsetAsync(reach_max_bits, 0, sizeof(unsigned) * (size_t)n_prob, st));
   if (n_tet <= 0) return 0;
-  k_tet_reach<<<(n_tet + 255) / 256, 256, 0, st>>>(sites, dim, cell_start, tet_sph, n_tet, reach, reach_max_bits);
+  k_tet_reach<<<(n_tet + 255) / 256, 256, 0, st>>>(sites, cell_start, probs, tet_prob, lone, tet_sph, n_tet, reach,
+                                                   reach_max_bits);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -419,16 +439,19 @@ int tet_reach(const float4* sites, int dim, const int* cell_start, const float4*
 // Tets by centroid cell (once per mesh and grid): counting sort of the tets
 // by the cell of their float32 centroid.
 // ---------------------------------------------------------------------------
-__global__ void k_tet_cells(const float4* __restrict__ verts, const int4* __restrict__ tets, int n_tet, int dim,
+__global__ void k_tet_cells(const float4* __restrict__ verts, const int4* __restrict__ tets, int n_tet,
+                            const ProbDesc* __restrict__ probs, const int* __restrict__ tet_prob, ProbDesc lone,
                             int* __restrict__ count, int* __restrict__ tcell) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tet) return;
+  int pt;
+  const ProbDesc P = prob_for(probs, tet_prob, t, lone, pt);
   int4 q = tets[t];
   float4 a = verts[q.x], b = verts[q.y], c = verts[q.z], d = verts[q.w];
   float x = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), d.x), 0.25f);
   float y = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), d.y), 0.25f);
   float z = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), d.z), 0.25f);
-  int cell = grid_cell(x, y, z, dim);
+  int cell = P.cell_off + grid_cell(x, y, z, P.dim);
   tcell[t] = cell;
   atomicAdd(count + cell, 1);
 }
@@ -468,12 +491,13 @@ int tet_spheres(const float4* verts, const int4* tets, const int* tet_order, int
   return 0;
 }
 
-int tets_by_cell(const float4* verts, const int4* tets, int n_tet, int dim, int* tet_cell_start, int* cell_fill,
-                 int* tcell, int* tet_order, int* scan_tmp, cudaStream_t st) {
-  long long nc = (long long)dim * dim * dim;
+int tets_by_cell(const float4* verts, const int4* tets, int n_tet, long long ncell, const ProbDesc* probs,
+                 const int* tet_prob, const ProbDesc& lone, int* tet_cell_start, int* cell_fill, int* tcell,
+                 int* tet_order, int* scan_tmp, cudaStream_t st) {
+  const long long nc = ncell;
   VGB_CUDA_TRY(cudaMemsetAsync(tet_cell_start, 0, sizeof(int) * (nc + 1), st));
   VGB_CUDA_TRY(cudaMemsetAsync(cell_fill, 0, sizeof(int) * nc, st));
-  k_tet_cells<<<(n_tet + 255) / 256, 256, 0, st>>>(verts, tets, n_tet, dim, tet_cell_start, tcell);
+  k_tet_cells<<<(n_tet + 255) / 256, 256, 0, st>>>(verts, tets, n_tet, probs, tet_prob, lone, tet_cell_start, tcell);
   VGB_CUDA_TRY(cudaGetLastError());
   if (scan_exclusive(tet_cell_start, tet_cell_start, nc + 1, scan_tmp, st)) return -2;
   k_tet_scatter<<<(n_tet + 255) / 256, 256, 0, st>>>(tcell, n_tet, tet_cell_start, cell_fill, tet_order);

@@ -119,8 +119,11 @@ extern "C" int vgb_knn_noalloc(const float* d_points, int n, int k, unsigned* d_
   k_na_pack<<<(n + 255) / 256, 256, 0, st>>>(d_points, n, in);
   VGB_CUDA_TRY(cudaGetLastError());
   // grid_sort clears the cell counters and fill counters it needs at zero
-  if (grid_sort(in, sorted, n, dim, cell_start, cell_fill, site_cell, scan_tmp, st)) return VGB_ERR_CUDA;
-  if (knn_sites(sorted, n, dim, cell_start, k, pos_of_id, d_knn, st)) return VGB_ERR_CUDA;
+  const ProbDesc lone = lone_problem(n, dim, 0, k);
+  if (grid_sort(in, sorted, n, (long long)dim * dim * dim, nullptr, nullptr, lone, cell_start, cell_fill, site_cell,
+                scan_tmp, st))
+    return VGB_ERR_CUDA;
+  if (knn_sites(sorted, n, cell_start, nullptr, nullptr, lone, k, pos_of_id, d_knn, st)) return VGB_ERR_CUDA;
   k_na_perm<<<(n + 255) / 256, 256, 0, st>>>(sorted, n, d_perm);
   VGB_CUDA_TRY(cudaGetLastError());
   return VGB_OK;

@@ -85,6 +85,42 @@ __host__ __device__ inline dmom4 make_dmom4(double x, double y, double z, double
   return r;
 }
 
+// One problem of a batch: where its sites, grid cells, tets, neighbour rows
+// and inside field sit in the batch's concatenated arrays.  A lone problem is
+// the batch of one with every offset zero.
+struct ProbDesc {
+  int site_off, n_site;  // sites [site_off, site_off + n_site), input and grid order
+  int cell_off, dim;     // grid cells [cell_off, cell_off + dim^3)
+  int tet_off, n_tet;    // tets [tet_off, tet_off + n_tet), ids and centroid-order positions
+  int K, fdim;           // neighbours per site; side of the inside field
+  long long knn_off;     // first neighbour entry (rows of K)
+  long long field_off;   // first inside flag
+  long long sat_off;     // first summed-table entry
+  float rt_max;          // largest tet bounding radius
+  int reserved;
+};
+
+inline ProbDesc lone_problem(int n_site, int dim, int n_tet, int K) {
+  ProbDesc d{};
+  d.n_site = n_site;
+  d.dim = dim;
+  d.n_tet = n_tet;
+  d.K = K;
+  return d;
+}
+
+// The problem of unit i (a site or a tet, by position) and its descriptor;
+// probs == nullptr selects `lone`.
+__device__ __forceinline__ ProbDesc prob_for(const ProbDesc* probs, const int* prob_of_unit, int i,
+                                             const ProbDesc& lone, int& p) {
+  if (probs == nullptr) {
+    p = 0;
+    return lone;
+  }
+  p = prob_of_unit[i];
+  return probs[p];
+}
+
 // --- host-side plumbing ----------------------------------------------------
 void set_error(const char* fmt, ...);
 const char* last_error();
@@ -104,35 +140,41 @@ const char* last_error();
 size_t scan_tmp_ints(long long n);
 int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t st);
 
-// Grid sort of n sites (float4 x,y,z,id) by (cell, id).
-//   cell_start: dim^3 + 1 ints; cell_fill, site_cell: scratch (dim^3, n ints).
-//   scan_tmp: scan_tmp_ints(dim^3 + 1) ints.
-int grid_sort(const float4* in, float4* out, int n, int dim, int* cell_start, int* cell_fill, int* site_cell,
-              int* scan_tmp, cudaStream_t st);
+// Grid sort of n sites (float4 x,y,z,id) by (cell, id); each site's cell is
+// its problem's cell_off + its cell in that problem's grid, so problems stay
+// in order and contiguous.
+//   cell_start: ncell + 1 ints; cell_fill, site_cell: scratch (ncell, n ints).
+//   scan_tmp: scan_tmp_ints(ncell + 1) ints.
+int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbDesc* probs, const int* site_prob,
+              const ProbDesc& lone, int* cell_start, int* cell_fill, int* site_cell, int* scan_tmp, cudaStream_t st);
 
 // K nearest sorted sites of every sorted site (self excluded) or of every tet
-// centroid, ordered by (distance, id).  Output rows are sorted-space indices.
-// pos_of_id: n ints, written by knn_sites (sorted position of each id) and
-// read by knn_tet_centroids.  Centroid queries come grouped by cell:
-// tet_order / tet_cell_start from tets_by_cell.
-int knn_sites(const float4* sites, int n, int dim, const int* cell_start, int k, int* pos_of_id, unsigned* out,
-              cudaStream_t st);
+// centroid, ordered by (distance, id).  Output rows are sorted-space indices
+// (positions in the batch's site array); a site's row is its problem's
+// knn_off + (position - site_off) * K.  pos_of_id: n ints, written by
+// knn_sites (position of each site_off + id) and read by knn_tet_centroids
+// (lone problem).  Centroid queries come grouped by cell: tet_order /
+// tet_cell_start from tets_by_cell.  kmax: the largest K of the problems.
+int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, cudaStream_t st);
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, cudaStream_t st);
 // Exact form: reach[q] = (distance from the centroid of the q-th tet in
-// centroid-cell order to its nearest site) + 2 (its bounding radius);
-// *reach_max_bits = float bits of the largest reach.  Sites grid-sorted,
-// tet_sph from tet_spheres.
-int tet_reach(const float4* sites, int dim, const int* cell_start, const float4* tet_sph, int n_tet, float* reach,
+// centroid-cell order to its nearest site of the same problem) + 2 (its
+// bounding radius); reach_max_bits[p] = float bits of problem p's largest
+// reach (n_prob entries).  Sites grid-sorted, tet_sph from tet_spheres.
+int tet_reach(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* tet_prob,
+              const ProbDesc& lone, int n_prob, const float4* tet_sph, int n_tet, float* reach,
               unsigned* reach_max_bits, cudaStream_t st);
 // Bounding spheres (centroid, radius) of the tets in centroid-cell order.
 int tet_spheres(const float4* verts, const int4* tets, const int* tet_order, int n_tet, float4* sph, cudaStream_t st);
-// Tets sorted by the grid cell of their float32 centroid (once per mesh):
-// tet_cell_start dim^3 + 1 ints, cell_fill dim^3 scratch, tcell n_tet scratch,
-// tet_order n_tet ints.
-int tets_by_cell(const float4* verts, const int4* tets, int n_tet, int dim, int* tet_cell_start, int* cell_fill,
-                 int* tcell, int* tet_order, int* scan_tmp, cudaStream_t st);
+// Tets sorted by the grid cell of their float32 centroid in their problem's
+// grid (once per mesh): tet_cell_start ncell + 1 ints, cell_fill ncell
+// scratch, tcell n_tet scratch, tet_order n_tet ints.
+int tets_by_cell(const float4* verts, const int4* tets, int n_tet, long long ncell, const ProbDesc* probs,
+                 const int* tet_prob, const ProbDesc& lone, int* tet_cell_start, int* cell_fill, int* tcell,
+                 int* tet_order, int* scan_tmp, cudaStream_t st);
 
 // Site-major lists of candidate tets: for each site, the tets whose candidate
 // row holds it.  start: n+1 ints, fill: n ints scratch, list: n_tet*tk ints.
@@ -141,18 +183,19 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 
 // Site-major clipping of every candidate pair -- the tet-cell method, or the
 // cell-tet method when cell_tet -- with per-site moments relative to the
-// site: mom[s] = (vol, mx, my, mz).
+// site: mom[s] = (vol, mx, my, mz).  Each site reads its problem's
+// descriptor (K, neighbour rows, grid, field, tets).
 // Exact form (cell-tet only; all of field, field_sat, tet_order and
 // tet_cell_start given): cells inside the mesh (field: fdim^3 inside flags,
 // field_sat: (fdim+1)^3 summed touched counts, from build_inside_field) are
 // taken whole, other cells are clipped by every tet within reach (tets sorted
 // by centroid cell of the site grid, dim^3 cells).  Otherwise the candidate
 // lists site_start / site_tets are used.
-int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, int k, const float4* verts,
-                    const int4* tets, const int* site_start, const int* site_tets, dmom4* mom,
-                    unsigned long long* stats, const unsigned char* field, const unsigned* field_sat, int fdim,
-                    const int* tet_order,
-                    const int* tet_cell_start, int dim, float rt_max, const float4* tet_sph, const float* reach,
+int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
+                    const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
+                    const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
+                    const unsigned char* field, const unsigned* field_sat, const int* tet_order,
+                    const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
