@@ -104,6 +104,16 @@ def lib() -> C.CDLL:
     L.vgb_host_free.argtypes = [vp]
     L.vgb_host_free.restype = None
     L.vgb_clipped_voro_diagram.argtypes = [vp, i, vp, i, vp, i, i, i, i, i, i]
+    L.vgb_batch_create.argtypes = [C.POINTER(vp), C.POINTER(_Config), i, vp, vp, vp, vp, vp, vp]
+    L.vgb_batch_destroy.argtypes = [vp]
+    L.vgb_batch_destroy.restype = None
+    L.vgb_batch_iterate.argtypes = [vp, i, i]
+    L.vgb_batch_sync.argtypes = [vp]
+    L.vgb_batch_time_iterate.argtypes = [vp, i, i, C.POINTER(C.c_float)]
+    L.vgb_batch_info.argtypes = [vp, ip, ip, ip, C.POINTER(C.c_float)]
+    L.vgb_batch_problem.argtypes = [vp, i, ip, ip, ip, ip, ip]
+    L.vgb_batch_get_problem.argtypes = [vp, i, vp, vp, vp]
+    L.vgb_batch_get_stats.argtypes = [vp, vp]
     L.kn_prepare_ex.argtypes = [C.POINTER(C.POINTER(_KnProblem)), vp, i, i]
     L.kn_solve_ex.argtypes = [C.POINTER(_KnProblem)]
     L.kn_free_ex.argtypes = [C.POINTER(_KnProblem)]
@@ -275,6 +285,93 @@ class Engine:
         _check(lib().vgb_engine_time_iterate(self._h, n_iter, int(update), C.byref(ms)),
                "vgb_engine_time_iterate")
         return ms.value
+
+
+class Batch:
+    """Many independent problems iterated together (exact cell-tet form).
+
+    problems: sequence of (verts (nv,3) float32, tets (nt,4) int32, sites (n,3)
+    float32), coordinates in [0,1000]^3.  site_k=0 lets the autotuner pick
+    each problem's K from 32, 48, 64, 96, 128; tune_grid lets it pick the grid
+    density by timing.  One launch per kernel per iteration covers the whole
+    batch; use_graph replays the iteration as a CUDA graph.
+    """
+
+    def __init__(self, problems, site_k: int = 0, tune_grid: bool = True, use_graph: bool = True,
+                 device: int = 0):
+        L = lib()
+        self._v = [_f32(v) for v, _, _ in problems]
+        self._t = [np.ascontiguousarray(t, dtype=np.int32) for _, t, _ in problems]
+        s = [_f32(x) for _, _, x in problems]
+        for t in self._t:
+            if t.ndim != 2 or t.shape[1] != 4:
+                raise ValueError("tets must be (nt, 4)")
+        P = len(problems)
+        vp_arr = (C.c_void_p * P)(*[_p(a) for a in self._v])
+        tp_arr = (C.c_void_p * P)(*[_p(a) for a in self._t])
+        sp_arr = (C.c_void_p * P)(*[_p(a) for a in s])
+        nv = (C.c_int * P)(*[len(a) for a in self._v])
+        nt = (C.c_int * P)(*[len(a) for a in self._t])
+        ns = (C.c_int * P)(*[len(a) for a in s])
+        cfg = _Config()
+        L.vgb_config_init(C.byref(cfg))
+        cfg.site_k, cfg.grid_dim = site_k, 0 if tune_grid else 1
+        cfg.method, cfg.use_graph, cfg.device, cfg.exact = METHODS["cell_tet"], int(use_graph), device, 1
+        h = C.c_void_p()
+        _check(L.vgb_batch_create(C.byref(h), C.byref(cfg), P, vp_arr, nv, tp_arr, nt, sp_arr, ns),
+               "vgb_batch_create")
+        self._h = h
+        n_prob, n_site, n_tet, dens = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        L.vgb_batch_info(h, C.byref(n_prob), C.byref(n_site), C.byref(n_tet), C.byref(dens))
+        self.n_prob, self.n_site, self.n_tet, self.density = n_prob.value, n_site.value, n_tet.value, dens.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().vgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def problem(self, p: int) -> dict:
+        """Sizes and tuned parameters of problem p."""
+        v = [C.c_int() for _ in range(5)]
+        _check(lib().vgb_batch_problem(self._h, p, *[C.byref(x) for x in v]), "vgb_batch_problem")
+        return dict(zip(("n_site", "n_tet", "site_k", "grid_dim", "field_dim"), (x.value for x in v)))
+
+    def iterate(self, n_iter: int = 1, update: bool = True):
+        _check(lib().vgb_batch_iterate(self._h, n_iter, int(update)), "vgb_batch_iterate")
+
+    def sync(self):
+        _check(lib().vgb_batch_sync(self._h), "vgb_batch_sync")
+
+    def time_iterate(self, n_iter: int, update: bool = True) -> float:
+        ms = C.c_float()
+        _check(lib().vgb_batch_time_iterate(self._h, n_iter, int(update), C.byref(ms)), "vgb_batch_time_iterate")
+        return ms.value
+
+    def result(self, p: int):
+        """(sites (n,3) float32, volumes (n,), first moments (n,3)) of problem p, input order."""
+        n = self.problem(p)["n_site"]
+        xyz = np.empty((n, 3), np.float32)
+        vol = np.empty(n, np.float64)
+        mom = np.empty((n, 3), np.float64)
+        _check(lib().vgb_batch_get_problem(self._h, p, _p(xyz), _p(vol), _p(mom)), "vgb_batch_get_problem")
+        return xyz, vol, mom
+
+    def stats(self) -> dict:
+        out = np.zeros(STAT_COUNT, np.uint64)
+        _check(lib().vgb_batch_get_stats(self._h, _p(out)), "vgb_batch_get_stats")
+        return {k: int(out[i]) for i, k in enumerate(STAT_NAMES)}
 
 
 class PinnedArray:

@@ -58,7 +58,8 @@ enum WarpCount : int {
 };
 
 struct SiteSmem {
-  float4 plane[4 + MAX_SITE_K + BOX_PLANES];  // 0..3 tet faces, 4+j bisector j, 4+K+b box face b
+  float4 plane[4 + MAX_SITE_K + 2 * BOX_PLANES];  // 0..3 tet faces, 4+j bisector j, 4+K+b start-cube
+                                                  // face b, 4+K+6+b domain-box face b
   unsigned conf[MAX_TRI];                     // clip scratch: removed triangles
   unsigned bedge[MAX_TRI];                    // clip scratch: boundary edges
   unsigned queue[WARP];                       // surviving candidate tets of a chunk
@@ -83,7 +84,7 @@ struct SiteSmem {
 //     reached (voronoi.cu:679-697): the cell-tet build and the tet-cell
 //     method's per-tet cells;
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
-template <bool CELL_TET>
+template <bool CELL_TET, bool BATCHED>
 __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     dmom4* __restrict__ mom, unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, const int* __restrict__ tet_order,
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
-    const unsigned* __restrict__ reach_max_bits) {
+    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss) {
   __shared__ SiteSmem smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -103,12 +104,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
   __syncwarp();
 
   for (int s = blockIdx.x * CLIP_WARPS + wib; s < n; s += gridDim.x * CLIP_WARPS) {
-    int pidx;
-    const ProbDesc P = prob_for(probs, site_prob, s, lone, pidx);
-    const int K = P.K;
+    // the site's problem; its descriptor fields are read where used (from
+    // global memory or the kernel parameters) rather than held in registers
+    const int pidx = BATCHED ? site_prob[s] : 0;
+#define PD(f) (BATCHED ? probs[pidx].f : lone.f)
+    const int K = PD(K);
     const float4 seed = sites[s];
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
-    const unsigned* krow = knn + P.knn_off + (size_t)(s - P.site_off) * K;
+    const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
     for (int j = lane; j < K; j += WARP) {
       float4 B = sites[krow[j]];
       float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
@@ -121,15 +124,26 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     // by a tet is the same, and the cube's edges are in general position (an
     // edge of the fixed box can lie exactly on mesh planes such as x = y,
     // where float rounding then splits the edge).
-    float L = 0.f;
+    // The reference's box itself (planes 4+K+6..) bounds the part of the
+    // cell that can meet a tet: it gives the security radius and the culling
+    // radius, while the cube-start cell is what the tets clip.
+    constexpr float lo = -0.1f, hi = 1000.1f;
+    auto cube_half = [&]() {
+      return fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
+                   fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
+    };
     if (CELL_TET) {
-      const float lo = -0.1f, hi = 1000.1f;
-      L = fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
-                fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
+      const float L = cube_half();
       if (lane < BOX_PLANES) {
         const int ax = lane >> 1;
         const float sgn = (lane & 1) ? -1.f : 1.f;
         S.plane[4 + K + lane] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
+      } else if (lane < 2 * BOX_PLANES) {
+        const int b = lane - BOX_PLANES, ax = b >> 1;
+        const float sgn = (b & 1) ? -1.f : 1.f;
+        const float sc = ax == 0 ? seed.x : ax == 1 ? seed.y : seed.z;
+        S.plane[4 + K + lane] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f,
+                                            (b & 1) ? hi - sc : sc - lo);
       }
     }
     __syncwarp();
@@ -137,7 +151,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     CompSum V, MX, MY, MZ;  // site-relative volume and first moment
     float Rc = 0.f;
     int nfaces = 0;
-    bool building = CELL_TET;  // the current cell is the site's own cell
+    // jobs: 0 build the site's cell; 1 bound it by the domain box (when its
+    // security radius was not reached); 2 clip the next candidate tet
+    int job = CELL_TET ? 0 : 2;
     // candidate scan: segments of a tet list, 32 tets per chunk
     int nseg = 0, nj = 1, i0 = 0, i1 = 0, j0 = 0, k0 = 0;
     int seg = -1, base = 0, se = 0, qi = 0, nsurv = 0;
@@ -145,10 +161,12 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
 
     while (true) {
       // ---------------------------------------------------------------
-      // the next cell: the site's cell, or the next surviving candidate
+      // the next cell: the site's cell, the same cell (from its shared copy)
+      // for the box bound, or the next surviving candidate
       WarpCell c;
       cell_clear(c);
-      if (building) {
+      if (job == 0) {
+        const float L = cube_half();
         if (lane < 8) {
           // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
           // ordered so each dual triangle has a negative normal determinant
@@ -163,13 +181,26 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         c.vm[0] = 0xffu;
         c.nt = 8;
         c.r2 = 3.f * L * L;
+      } else if (job == 1) {
+#pragma unroll
+        for (int k = 0; k < TRI_SLOTS; ++k) {
+          c.vm[k] = S.mvm[k];
+          if (c.vm[k] & lane_bit) {
+            c.tri[k] = S.mtri[k * WARP + lane];
+            const float4 v = S.mv[k * WARP + lane];
+            c.vx[k] = v.x; c.vy[k] = v.y; c.vz[k] = v.z; c.vw[k] = v.w;
+          }
+        }
+        c.nt = S.mnt;
+        c.r2 = S.mr2;
       } else {
         // refill the queue from the next chunk(s) of candidates
         while (qi >= nsurv) {
           if (base >= se) {
             if (++seg >= nseg) break;
             if (exact) {
-              const int row = P.cell_off + P.dim * ((j0 + seg % nj) + P.dim * (k0 + seg / nj));
+              const int pd = PD(dim);
+              const int row = PD(cell_off) + pd * ((j0 + seg % nj) + pd * (k0 + seg / nj));
               base = tet_cell_start[i0 + row];
               se = tet_cell_start[i1 + row + 1];
             } else {
@@ -308,13 +339,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
       }
 
       // ---------------------------------------------------------------
-      // the plane sequence: bisectors until the security radius, or the
-      // tet's four faces
-      const bool bis = building || !CELL_TET;
-      const int pend = bis ? 4 + K : 4;
+      // the plane sequence: bisectors until the security radius, the six
+      // domain-box faces, or the tet's four faces
+      const bool bis = job == 0 || !CELL_TET;
+      const int pbeg = job == 1 ? 4 + K + BOX_PLANES : bis ? 4 : 0;
+      const int pend = job == 1 ? pbeg + BOX_PLANES : bis ? 4 + K : 4;
       int state = 0;  // 0 kept, 1 empty, 2 dropped
       bool secmiss = bis;
-      for (int pi = bis ? 4 : 0; pi < pend; ++pi) {
+      for (int pi = pbeg; pi < pend; ++pi) {
         const float4 P = S.plane[pi];
         if (lane == 0) { S.cnt[WC_PLANES]++; S.cnt[WC_CONFLICT] += (unsigned)c.nt; }
         const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane);
@@ -328,13 +360,11 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         // |neighbour - site|^2 > 4 max|v - site|^2
         if (bis && 2.f * P.w > 4.f * c.r2) { secmiss = false; break; }
       }
-      if (bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
+      if (job == 2 && bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
 
       // ---------------------------------------------------------------
       bool take = state == 0, interior = false;
-      if (building) {
-        building = false;
-        take = false;
+      if (job == 0) {
         if (state != 0) break;  // the site's cell failed: no tet is clipped
 #pragma unroll
         for (int k = 0; k < TRI_SLOTS; ++k)
@@ -344,22 +374,55 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
           }
         if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
         if (lane == 0) { S.mnt = c.nt; S.mr2 = c.r2; }
+        __syncwarp();
+        if (secmiss) {
+          job = 1;
+          continue;
+        }
+      } else if (job == 1) {
+        if (state == 1) break;  // the cell misses the domain box: no tet meets it
+      }
+      if (job != 2) {
+        const bool build_miss = job == 1;
+        job = 2;
+        take = false;
+        if (state != 0) {
+          // the box bound failed (degenerate): keep the unbounded cell
+#pragma unroll
+          for (int k = 0; k < TRI_SLOTS; ++k) {
+            c.vm[k] = S.mvm[k];
+            if (c.vm[k] & lane_bit) {
+              c.tri[k] = S.mtri[k * WARP + lane];
+              const float4 v = S.mv[k * WARP + lane];
+              c.vx[k] = v.x; c.vy[k] = v.y; c.vz[k] = v.z; c.vw[k] = v.w;
+            }
+          }
+          c.nt = S.mnt;
+          c.r2 = S.mr2;
+        }
+        // |K-th neighbour - site|^2 > 4 max|v - site|^2 over the bounded cell
+        const bool secmiss = build_miss && !(2.f * S.plane[4 + K - 1].w > 4.f * c.r2);
+        if (secmiss && lane == 0) {
+          S.cnt[WC_SECMISS]++;
+          if (prob_secmiss) atomicAdd(prob_secmiss + pidx, 1u);
+        }
         Rc = sqrtf(c.r2);
         // A cell that provably lies inside the mesh is its own clipped cell:
         // the sum over the tets it meets of (cell ^ tet) is the cell itself.
         // The cell lies within Rc of its site; when the box of field cells
         // covering that ball holds no cell touched by the mesh boundary and
-        // the site's field cell is inside, the ball is inside the mesh.
+        // the site's field cell is inside, the ball is inside the mesh (and
+        // inside the domain box, so the bound above left the cell as built).
         const float Rq = Rc * 1.001f + 0.01f;
-        const int fdim = P.fdim;
+        const int fdim = field ? PD(fdim) : 1;
         if (field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
             seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f &&
-            field[P.field_off + grid_cell(seed.x, seed.y, seed.z, fdim)]) {
+            field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]) {
           const int a0 = grid_axis(seed.x - Rq, fdim), a1 = grid_axis(seed.x + Rq, fdim) + 1;
           const int b0 = grid_axis(seed.y - Rq, fdim), b1 = grid_axis(seed.y + Rq, fdim) + 1;
           const int c0 = grid_axis(seed.z - Rq, fdim), c1 = grid_axis(seed.z + Rq, fdim) + 1;
           const size_t W = (size_t)fdim + 1;
-          const unsigned* sat = field_sat + P.sat_off;
+          const unsigned* sat = field_sat + PD(sat_off);
           auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
           const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
                                    at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
@@ -392,8 +455,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
           // centroid within Rc + rt_max of the site, and no tet reaches
           // farther than the largest reach
           if (exact) {
-            const int dim = P.dim;
-            const float R = fminf(Rc + P.rt_max * 1.001f, __uint_as_float(reach_max_bits[pidx])) + 0.01f;
+            const int dim = PD(dim);
+            const float R = fminf(Rc + PD(rt_max) * 1.001f, __uint_as_float(reach_max_bits[pidx])) + 0.01f;
             i0 = grid_axis(seed.x - R, dim);
             i1 = grid_axis(seed.x + R, dim);
             j0 = grid_axis(seed.y - R, dim);
@@ -425,6 +488,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
     }
     if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
     __syncwarp();
+#undef PD
   }
   const unsigned cull_warp = __reduce_add_sync(FULL, cull_lane);
   if (lane == 0) S.cnt[WC_CULLTESTS] += cull_warp;
@@ -438,16 +502,18 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
   }
 }
 
-static int g_clip_resident_blocks[2] = {0, 0};  // SMs x resident blocks per SM, per method
+static int g_clip_resident_blocks[3] = {0, 0, 0};  // SMs x resident blocks per SM, per variant
 
 int clip_prepare() {
   int dev = 0, sms = 0, per_sm = 0;
   VGB_CUDA_TRY(cudaGetDevice(&dev));
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<false>, CLIP_WARPS * WARP, 0));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<false, false>, CLIP_WARPS * WARP, 0));
   g_clip_resident_blocks[0] = sms * (per_sm > 0 ? per_sm : 1);
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<true>, CLIP_WARPS * WARP, 0));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<true, false>, CLIP_WARPS * WARP, 0));
   g_clip_resident_blocks[1] = sms * (per_sm > 0 ? per_sm : 1);
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<true, true>, CLIP_WARPS * WARP, 0));
+  g_clip_resident_blocks[2] = sms * (per_sm > 0 ? per_sm : 1);
   return 0;
 }
 
@@ -456,22 +522,33 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, cudaStream_t st) {
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
+  if (!cell_tet && probs) {
+    set_error("the tet-cell method runs one problem at a time");
+    return -1;
+  }
   // a few waves of resident blocks; sites are dealt round-robin to warps
-  long long want = (long long)g_clip_resident_blocks[cell_tet ? 1 : 0] * 4;
+  const int variant = !cell_tet ? 0 : probs ? 2 : 1;
+  long long want = (long long)g_clip_resident_blocks[variant] * 4;
   long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
   int blocks = (int)(want < need ? want : need);
-  if (cell_tet)
-    k_clip_site<true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
-                                                            site_start, site_tets, mom, stats, field, field_sat,
-                                                            tet_order, tet_cell_start, tet_sph, reach,
-                                                            reach_max_bits);
+  if (variant == 2)
+    k_clip_site<true, true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
+                                                                  site_start, site_tets, mom, stats, field,
+                                                                  field_sat, tet_order, tet_cell_start, tet_sph,
+                                                                  reach, reach_max_bits, prob_secmiss);
+  else if (variant == 1)
+    k_clip_site<true, false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts,
+                                                                   tets, site_start, site_tets, mom, stats, field,
+                                                                   field_sat, tet_order, tet_cell_start, tet_sph,
+                                                                   reach, reach_max_bits, prob_secmiss);
   else
-    k_clip_site<false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
-                                                             site_start, site_tets, mom, stats, nullptr, nullptr,
-                                                             nullptr, nullptr, nullptr, nullptr, nullptr);
+    k_clip_site<false, false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts,
+                                                                    tets, site_start, site_tets, mom, stats, nullptr,
+                                                                    nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                                    nullptr, prob_secmiss);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -118,6 +118,13 @@ __global__ void k_finish(float4* __restrict__ sites, int n, dmom4* __restrict__ 
   mom[s] = m;
 }
 
+int finish_sites(float4* sites, int n, dmom4* mom, int update, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_finish<<<(n + 255) / 256, 256, 0, st>>>(sites, n, mom, update);
+  VGB_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 // Plain form: float moments are already absolute; convert to the double layout.
 __global__ void k_finish_plain(float4* __restrict__ sites, int n, const float4* __restrict__ mf,
                                dmom4* __restrict__ mom, int update) {
@@ -205,7 +212,7 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
-                        e->reach_max, st))
+                        e->reach_max, nullptr, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,

@@ -464,6 +464,24 @@ __global__ void k_tet_scatter(const int* __restrict__ tcell, int n_tet, const in
   order[start[c] + atomicAdd(fill + c, 1)] = t;
 }
 
+// Tets of each cell in id order (insertion sort; a few dozen per cell), so
+// the order in which a cell's pieces are summed does not depend on the
+// scatter's atomics.
+__global__ void k_tet_cell_order(int* __restrict__ order, const int* __restrict__ start, long long ncell) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = start[c], e = start[c + 1];
+  for (int i = b + 1; i < e; ++i) {
+    const int x = order[i];
+    int j = i - 1;
+    while (j >= b && order[j] > x) {
+      order[j + 1] = order[j];
+      --j;
+    }
+    order[j + 1] = x;
+  }
+}
+
 // Bounding sphere (centroid, largest corner distance) of each tet, in
 // centroid-cell order (exact form, once per mesh).
 __global__ void k_tet_spheres(const float4* __restrict__ verts, const int4* __restrict__ tets,
@@ -501,6 +519,7 @@ int tets_by_cell(const float4* verts, const int4* tets, int n_tet, long long nce
   VGB_CUDA_TRY(cudaGetLastError());
   if (scan_exclusive(tet_cell_start, tet_cell_start, nc + 1, scan_tmp, st)) return -2;
   k_tet_scatter<<<(n_tet + 255) / 256, 256, 0, st>>>(tcell, n_tet, tet_cell_start, cell_fill, tet_order);
+  k_tet_cell_order<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(tet_order, tet_cell_start, nc);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -196,7 +196,12 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, cudaStream_t st);
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, cudaStream_t st);
+// prob_secmiss (optional): per-problem count of sites whose cell never
+// reached the security radius.
+
+// Absolute moments and the Lloyd update of n sites (engine.cu).
+int finish_sites(float4* sites, int n, dmom4* mom, int update, cudaStream_t st);
 
 // Reference-layout clipping: one thread per (tet, slot) pair, tet-major, float
 // atomics into per-site sums (the plain form).  mom_f: n float4 (vol, m).

@@ -224,6 +224,20 @@ def cube_problem(n_cells: int = 20, n_site: int = 20000, seed: int = 1, jitter: 
     return Problem(f"kuhn{n_cells}_s{n_site}", v, tets.astype(np.int32), s)
 
 
+def batch_problems(n_prob: int = 256, seed: int = 4, cells: tuple = (4, 48), sites: tuple = (500, 200_000),
+                   jitter: float = 0.1) -> list:
+    """Independent Kuhn cubes for the batched form: side n uniform in
+    [cells], interior vertices jittered by +-jitter grid spacings, sites
+    log-uniform in [sites], uniform in the cube."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(n_prob):
+        n = int(rng.integers(cells[0], cells[1] + 1))
+        ns = int(np.exp(rng.uniform(np.log(sites[0]), np.log(sites[1]))))
+        out.append(cube_problem(n, ns, seed=int(rng.integers(1 << 31)), jitter=jitter))
+    return out
+
+
 _TORUS_CACHE: dict = {}
 
 

@@ -29,6 +29,7 @@ CPU by oracle/make_ref.py), on a bounded sample of each step.
 from __future__ import annotations
 
 import argparse
+import collections
 import importlib.util
 import json
 import os
@@ -61,6 +62,11 @@ WORKLOADS = {
     # the small configuration
     "kuhn20_20k": dict(kind="cube", cells=20, n=20000, K=64,
                        desc="unit cube, 20^3 Kuhn grid (48,000 tets); 20,000 uniform sites; K=64"),
+    # the batched configuration: many independent problems per launch
+    "batch256_kuhn": dict(kind="batch", n_prob=256, K=0,
+                          desc="256 independent Kuhn cubes, side n uniform in [4,48], interior jitter 0.1 spacing; "
+                               "sites log-uniform in [500, 200000] per problem, uniform in the cube; K autotuned "
+                               "in {32,48,64,96} per problem, grid density autotuned"),
 }
 DEFAULT_WORKLOAD = "torus128_uniform_1m"
 LAUNCHES_PER_STEP = {"cell_tet": 16, "site_major": 16, "plain": 11}
@@ -415,8 +421,71 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """The batched form: every problem of the batch advances one Lloyd
+    iteration per step, one launch per kernel for the whole batch."""
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = tdist
+    pkg = load_package()
+    pkg.build()
+    import voronoi_gb300.meshgen as mg
+    w = WORKLOADS[args.workload]
+    probs = mg.batch_problems(w["n_prob"], seed=4)
+    t0 = time.perf_counter()
+    B = pkg.Batch([(P.verts, P.tets, P.sites) for P in probs], site_k=0, tune_grid=True, use_graph=True,
+                  device=local)
+    create_s = time.perf_counter() - t0
+    B.time_iterate(args.warmup, update=True)
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = B.time_iterate(args.steps, update=True)
+    clk = clocks.stop()
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1e3)
+    stats = B.stats()
+    ks = collections.Counter(B.problem(p)["site_k"] for p in range(B.n_prob))
+    n_site, n_tet, n_prob, dens = B.n_site, B.n_tet, B.n_prob, B.density
+    B.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "n_prob": n_prob, "n_site": n_site,
+                   "n_tet": n_tet, "site_k_histogram": {str(k): v for k, v in sorted(ks.items())},
+                   "grid_density": round(dens, 2), "form": "exact, batched (one launch per kernel per iteration)",
+                   "cuda_graph": True, "create_s": round(create_s, 2), "l2": "inputs larger than L2, no flush",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": 11 * args.steps,
+        "e2e": None,
+        "sites_per_s": round(n_site * value / world, 1),
+        "stats": stats,
+        "clocks": clk,
+        "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world, rank, local = dist_env()
+    if WORKLOADS[args.workload]["kind"] == "batch":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form: it runs one "
+                              "mesh and one site set per call"}), flush=True)
+        return
     if rank != 0:
         return
     checker = load_checker()
@@ -496,6 +565,8 @@ def main():
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOADS[args.workload]["kind"] == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -203,6 +203,37 @@ int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const int* indic
 #define VGB_NOALLOC_MAX_POINTS 65536
 int vgb_knn_noalloc(const float* d_points, int n, int k, unsigned* d_knn, unsigned* d_perm, void* stream);
 
+/* ---- Batched form --------------------------------------------------------
+ * No counterpart in the reference, which runs one mesh and one site set per
+ * call (voronoi.h:78-84).  Many independent problems -- problem p is a tet
+ * mesh (verts[p]: n_vert[p] x 3 floats, tets[p]: n_tet[p] x 4 ints) and its
+ * sites (sites[p]: n_site[p] x 3 floats), coordinates in [0,1000]^3 -- are
+ * iterated together: one launch per kernel per Lloyd iteration covers every
+ * site of every problem (exact cell-tet form), and with cfg->use_graph the
+ * iteration is a CUDA graph.  cfg->site_k = 0 lets the autotuner pick each
+ * problem's K: the smallest of 32, 48, 64, 96, 128 (at most n_site - 1) whose
+ * cells all reach the security radius, which gives the result of any larger
+ * K.  cfg->grid_dim = 0 lets it pick the grid density (sites per cell) by
+ * timing 1.5, 3.1 and 6; any other value keeps the reference's 3.1. */
+typedef struct vgb_batch vgb_batch;
+int vgb_batch_create(vgb_batch** out, const vgb_config* cfg, int n_prob, const float* const* verts,
+                     const int* n_vert, const int* const* tets, const int* n_tet, const float* const* sites,
+                     const int* n_site);
+void vgb_batch_destroy(vgb_batch* b);
+int vgb_batch_iterate(vgb_batch* b, int n_iter, int update);
+int vgb_batch_sync(vgb_batch* b);
+/* n_iter iterations timed with CUDA events on the batch's stream. */
+int vgb_batch_time_iterate(vgb_batch* b, int n_iter, int update, float* ms);
+int vgb_batch_info(const vgb_batch* b, int* n_prob, int* n_site_total, int* n_tet_total, float* density);
+/* Sizes and the tuned parameters of problem p. */
+int vgb_batch_problem(const vgb_batch* b, int p, int* n_site, int* n_tet, int* site_k, int* grid_dim,
+                      int* field_dim);
+/* Sites (n_site x 3), volumes and first moments (n_site x 3) of problem p in
+ * its input order; any pointer may be NULL. */
+int vgb_batch_get_problem(vgb_batch* b, int p, float* xyz, double* vol, double* mom);
+/* Counters of the last pass over the whole batch: out[VGB_STAT_COUNT]. */
+int vgb_batch_get_stats(vgb_batch* b, unsigned long long* out);
+
 #ifdef __cplusplus
 }
 #endif
