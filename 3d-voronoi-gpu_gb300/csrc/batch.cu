@@ -155,8 +155,8 @@ int layout(vgb_batch* b) {
 int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   cudaStream_t st = b->st;
   const ProbDesc none{};
-  if (grid_sort(b->sites, b->sites_tmp, b->n, b->ncell, b->d_probs, b->site_prob, none, b->cell_start, b->cell_fill,
-                b->site_cell, b->scan_tmp, st))
+  if (grid_sort(b->sites, b->sites_tmp, b->n, b->ncell, b->d_probs, b->site_prob, none, b->cell_start, b->site_cell,
+                st))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(b->sites, b->sites_tmp, sizeof(float4) * b->n, cudaMemcpyDeviceToDevice, st));
   if (knn_sites(b->sites, b->n, b->cell_start, b->d_probs, b->site_prob, none, b->kmax, b->pos_of_id, b->knn, st))
@@ -331,7 +331,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
   if ((rc = balloc(&b->d_probs, n_prob)) || (rc = balloc(&b->site_prob, b->n)) || (rc = balloc(&b->tet_prob, b->n_tet)) ||
       (rc = balloc(&b->verts, b->n_vert)) || (rc = balloc(&b->tets, b->n_tet)) || (rc = balloc(&b->sites, b->n)) ||
       (rc = balloc(&b->sites_tmp, b->n)) || (rc = balloc(&b->cell_start, cell_cap + 1)) ||
-      (rc = balloc(&b->cell_fill, cell_cap)) || (rc = balloc(&b->site_cell, b->n)) ||
+      (rc = balloc(&b->cell_fill, cell_cap)) || (rc = balloc(&b->site_cell, grid_sort_work_ints(b->n, cell_cap))) ||
       (rc = balloc(&b->scan_tmp, scan_tmp_ints((long long)scan_n))) || (rc = balloc(&b->pos_of_id, b->n)) ||
       (rc = balloc(&b->tet_order, b->n_tet)) || (rc = balloc(&b->tet_cell_start, cell_cap + 1)) ||
       (rc = balloc(&b->tcell, b->n_tet)) || (rc = balloc(&b->knn, knn_cap)) || (rc = balloc(&b->mom, b->n)) ||

@@ -6,15 +6,15 @@
 //   tets       int4[m]
 //   sites      float4[n]             x, y, z, original id (int bits), grid order
 //   sites_tmp  float4[n]             sort target
-//   cell_start int32[dim^3 + 1]      cell_fill int32[dim^3], site_cell int32[n]
+//   cell_start int32[dim^3 + 1]      cell_fill int32[dim^3], grid-sort work (2n + digit counts)
 //   knn        uint32[n][K]          row-major, grid order (knearests.h:15)
 //   cand       uint32[m][tk]         row-major (the reference keeps tk pitched rows)
 //   site_start int32[n + 1], site_fill int32[n], site_tets int32[m * tk]
 //   mom        dmom4[n]            volume, first moment
 //   stats      uint64[16]
-// One Lloyd iteration = grid sort -> kNN -> candidates -> site-major lists ->
-// clip -> update, all on one stream; with use_graph the iteration is captured
-// once and replayed.
+// One Lloyd iteration = grid sort -> kNN -> per-tet reach (exact form) or
+// candidates -> site-major lists (reference form) -> clip -> update, all on
+// one stream; with use_graph the iteration is captured once and replayed.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -37,7 +37,7 @@ struct vgb_engine {
   float4* sites_tmp = nullptr;
   int* cell_start = nullptr;
   int* cell_fill = nullptr;
-  int* site_cell = nullptr;
+  int* site_cell = nullptr;       // grid-sort work array (keys, digit counts, scan scratch)
   int* scan_tmp = nullptr;
   int* pos_of_id = nullptr;
   int* tet_order = nullptr;       // tets sorted by centroid cell
@@ -183,8 +183,7 @@ int run_pass(vgb_engine* e, int update) {
 #define MARK(i) \
   if (e->timed) VGB_CUDA_TRY(cudaEventRecord(e->ev[i], st))
   MARK(0);
-  if (grid_sort(e->sites, e->sites_tmp, e->n, e->ncell, nullptr, nullptr, e->prob, e->cell_start, e->cell_fill,
-                e->site_cell, e->scan_tmp, st))
+  if (grid_sort(e->sites, e->sites_tmp, e->n, e->ncell, nullptr, nullptr, e->prob, e->cell_start, e->site_cell, st))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(e->sites, e->sites_tmp, sizeof(float4) * e->n, cudaMemcpyDeviceToDevice, st));
   MARK(1);
@@ -338,7 +337,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   size_t scan_n = std::max((size_t)e->ncell + 1, (size_t)n_site + 1);
   if ((rc = dalloc(&e->verts, n_vert)) || (rc = dalloc(&e->tets, n_tet)) || (rc = dalloc(&e->sites, n_site)) ||
       (rc = dalloc(&e->sites_tmp, n_site)) || (rc = dalloc(&e->cell_start, e->ncell + 1)) ||
-      (rc = dalloc(&e->cell_fill, e->ncell)) || (rc = dalloc(&e->site_cell, n_site)) ||
+      (rc = dalloc(&e->cell_fill, e->ncell)) || (rc = dalloc(&e->site_cell, grid_sort_work_ints(n_site, e->ncell))) ||
       (rc = dalloc(&e->scan_tmp, scan_tmp_ints((long long)scan_n))) || (rc = dalloc(&e->pos_of_id, n_site)) ||
       (rc = dalloc(&e->tet_order, n_tet)) || (rc = dalloc(&e->tet_cell_start, e->ncell + 1)) ||
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||

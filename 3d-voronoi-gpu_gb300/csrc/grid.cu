@@ -1,16 +1,19 @@
-// Uniform-grid build over the sites: atomic count per cell, device exclusive
-// scan, scatter, then a per-cell pass that orders each cell's sites by id so
-// the sorted order is deterministic.  Replaces kn_firstbuild's count /
-// reserve / store (knearests.cu:29-57, 149-198), whose `reserve` hands out
-// cell ranges in atomic order and whose `store` leaves the order inside a cell
-// to the scheduler.
+// Uniform-grid build over the sites, ordered by (cell, id) so the order is
+// deterministic: the sites are gathered into id order with their cell keys,
+// then stably radix-sorted by cell (8-bit digits, as many passes as the cell
+// count needs: 3 at 1M sites); cell starts come from an atomic count and a
+// device exclusive scan.  Replaces kn_firstbuild's count / reserve / store
+// (knearests.cu:29-57, 149-198), whose `reserve` hands out cell ranges in
+// atomic order and whose `store` leaves the order inside a cell to the
+// scheduler.  The cost per site does not depend on how many sites share a
+// cell (dense clusters put thousands in one).
 //
-// HBM traffic per site: read 16 B (count) + 16 B (scatter) + 16 B (per-cell
-// pass), write 16 B (scatter) + 16 B (per-cell pass, only when a cell is out
-// of order) + 4 B cell id written and read back; cell arrays 12 B per cell.
+// HBM traffic per site: 16 B read + 20 B written by the gather, then per pass
+// 4 B (histogram) + 20 B read and 20 B written (scatter).
 #include <cstdarg>
 #include <cstdio>
 #include <mutex>
+#include <utility>
 
 #include "vgb_common.cuh"
 
@@ -125,63 +128,112 @@ int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t 
 // ---------------------------------------------------------------------------
 // Grid sort.
 // ---------------------------------------------------------------------------
-__global__ void k_grid_count(const float4* __restrict__ in, int n, const ProbDesc* __restrict__ probs,
-                             const int* __restrict__ site_prob, ProbDesc lone, int* __restrict__ count,
-                             int* __restrict__ site_cell) {
+// Sites into id order (position site_off + id of their problem) with their
+// global cell keys; cell populations counted.
+__global__ void k_grid_gather(const float4* __restrict__ in, int n, const ProbDesc* __restrict__ probs,
+                              const int* __restrict__ site_prob, ProbDesc lone, int* __restrict__ count,
+                              unsigned* __restrict__ key, float4* __restrict__ val) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int pb;
   const ProbDesc P = prob_for(probs, site_prob, i, lone, pb);
-  float4 p = in[i];
-  int c = P.cell_off + grid_cell(p.x, p.y, p.z, P.dim);
-  site_cell[i] = c;
+  const float4 p = in[i];
+  const unsigned c = (unsigned)(P.cell_off + grid_cell(p.x, p.y, p.z, P.dim));
+  const int dst = P.site_off + site_id(p);
+  key[dst] = c;
+  val[dst] = p;
   atomicAdd(count + c, 1);
 }
 
-__global__ void k_grid_scatter(const float4* __restrict__ in, int n, const int* __restrict__ site_cell,
-                               const int* __restrict__ start, int* __restrict__ fill, float4* __restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int c = site_cell[i];
-  int pos = start[c] + atomicAdd(fill + c, 1);
-  out[pos] = in[i];
+// Digit histogram of one tile of RADIX_TILE keys per warp, written bucket-major
+// (counts[digit * ntiles + tile]) so one exclusive scan gives every tile's
+// output offset per digit.
+constexpr int RADIX_WARPS = 8;
+
+__global__ void __launch_bounds__(RADIX_WARPS * 32) k_radix_hist(const unsigned* __restrict__ key, int n, int shift,
+                                                                 int ntiles, int* __restrict__ counts) {
+  __shared__ int hist[RADIX_WARPS][RADIX_BUCKETS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * RADIX_WARPS + w;
+  for (int d = lane; d < RADIX_BUCKETS; d += 32) hist[w][d] = 0;
+  __syncwarp();
+  if (tile < ntiles) {
+    const int b = tile * RADIX_TILE, e = min(n, b + RADIX_TILE);
+    for (int i = b + lane; i < e; i += 32) atomicAdd(&hist[w][(key[i] >> shift) & (RADIX_BUCKETS - 1)], 1);
+    __syncwarp();
+    for (int d = lane; d < RADIX_BUCKETS; d += 32) counts[(size_t)d * ntiles + tile] = hist[w][d];
+  }
 }
 
-// Order the sites of each cell by id (insertion sort; cells hold a few sites
-// on average, dense clusters a few hundred).
-__global__ void k_cell_order(float4* __restrict__ pts, const int* __restrict__ start, int ncell) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  int b = start[c], e = start[c + 1];
-  if (e - b < 2) return;
-  bool sorted = true;
-  for (int i = b + 1; i < e && sorted; ++i) sorted = site_id(pts[i - 1]) < site_id(pts[i]);
-  if (sorted) return;
-  for (int i = b + 1; i < e; ++i) {
-    float4 x = pts[i];
-    int k = site_id(x);
-    int j = i - 1;
-    while (j >= b && site_id(pts[j]) > k) {
-      pts[j + 1] = pts[j];
-      --j;
+// Stable scatter of one tile per warp: the tile's keys are taken 32 at a time
+// in order; equal digits inside a step are ranked by lane (match_any), and a
+// per-digit running offset carries the order across steps.
+__global__ void __launch_bounds__(RADIX_WARPS * 32) k_radix_scatter(const unsigned* __restrict__ key_in,
+                                                                    const float4* __restrict__ val_in, int n,
+                                                                    int shift, int ntiles,
+                                                                    const int* __restrict__ offsets,
+                                                                    unsigned* __restrict__ key_out,
+                                                                    float4* __restrict__ val_out) {
+  __shared__ int next[RADIX_WARPS][RADIX_BUCKETS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * RADIX_WARPS + w;
+  if (tile >= ntiles) return;  // whole warp
+  for (int d = lane; d < RADIX_BUCKETS; d += 32) next[w][d] = offsets[(size_t)d * ntiles + tile];
+  __syncwarp();
+  const unsigned lt = (1u << lane) - 1u;
+  const int b = tile * RADIX_TILE, e = min(n, b + RADIX_TILE);
+  for (int i0 = b; i0 < e; i0 += 32) {
+    const int i = i0 + lane;
+    const bool valid = i < e;
+    const unsigned k = valid ? key_in[i] : 0u;
+    const int d = valid ? (int)((k >> shift) & (RADIX_BUCKETS - 1)) : RADIX_BUCKETS + lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int pos = valid ? next[w][d] + __popc(peers & lt) : 0;
+    __syncwarp();
+    if (valid && (peers & lt) == 0u) next[w][d] += __popc(peers);
+    __syncwarp();
+    if (valid) {
+      key_out[pos] = k;
+      val_out[pos] = val_in[i];
     }
-    pts[j + 1] = x;
   }
 }
 
 int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int* cell_start, int* cell_fill, int* site_cell, int* scan_tmp, cudaStream_t st) {
+              const ProbDesc& lone, int* cell_start, int* work, cudaStream_t st) {
   VGB_CUDA_TRY(cudaMemsetAsync(cell_start, 0, sizeof(int) * (ncell + 1), st));
-  VGB_CUDA_TRY(cudaMemsetAsync(cell_fill, 0, sizeof(int) * ncell, st));
+  const long long ntiles = grid_sort_tiles(n);
+  unsigned* key_a = reinterpret_cast<unsigned*>(work);
+  unsigned* key_b = key_a + n;
+  int* counts = reinterpret_cast<int*>(key_b + n);
+  int* scan_tmp = counts + RADIX_BUCKETS * ntiles;
+  // digits needed for the largest cell key
+  int passes = 0;
+  for (long long top = ncell > 1 ? ncell - 1 : 0; top > 0; top >>= RADIX_BITS) ++passes;
+  // ping-pong so that the last pass writes `out`: the gather fills `out` for
+  // an even count, the source array (no longer needed) for an odd one --
+  // except that the gather cannot write its own source, so an odd count
+  // starts in `out` and finishes with a copy
+  float4* va = out;
+  float4* vb = const_cast<float4*>(in);
   if (n > 0) {
-    k_grid_count<<<(n + 255) / 256, 256, 0, st>>>(in, n, probs, site_prob, lone, cell_start, site_cell);
+    k_grid_gather<<<(n + 255) / 256, 256, 0, st>>>(in, n, probs, site_prob, lone, cell_start, key_a, va);
     VGB_CUDA_TRY(cudaGetLastError());
   }
   if (scan_exclusive(cell_start, cell_start, ncell + 1, scan_tmp, st)) return -2;
   if (n > 0) {
-    k_grid_scatter<<<(n + 255) / 256, 256, 0, st>>>(in, n, site_cell, cell_start, cell_fill, out);
-    k_cell_order<<<(int)((ncell + 255) / 256), 256, 0, st>>>(out, cell_start, (int)ncell);
-    VGB_CUDA_TRY(cudaGetLastError());
+    const int blocks = (int)((ntiles + RADIX_WARPS - 1) / RADIX_WARPS);
+    for (int ps = 0; ps < passes; ++ps) {
+      const int shift = ps * RADIX_BITS;
+      k_radix_hist<<<blocks, RADIX_WARPS * 32, 0, st>>>(key_a, n, shift, (int)ntiles, counts);
+      VGB_CUDA_TRY(cudaGetLastError());
+      if (scan_exclusive(counts, counts, (long long)RADIX_BUCKETS * ntiles, scan_tmp, st)) return -2;
+      k_radix_scatter<<<blocks, RADIX_WARPS * 32, 0, st>>>(key_a, va, n, shift, (int)ntiles, counts, key_b, vb);
+      VGB_CUDA_TRY(cudaGetLastError());
+      std::swap(key_a, key_b);
+      std::swap(va, vb);
+    }
+    if (va != out) VGB_CUDA_TRY(cudaMemcpyAsync(out, va, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st));
   }
   return 0;
 }

@@ -20,7 +20,7 @@ struct KnImpl {
   float4* sorted = nullptr;  // grid order with ids
   int* cell_start = nullptr;
   int* cell_fill = nullptr;
-  int* site_cell = nullptr;
+  int* grid_work = nullptr;  // grid_sort_work_ints(n, cells)
   int* scan_tmp = nullptr;
   int* pos_of_id = nullptr;
 };
@@ -54,7 +54,7 @@ void kn_release(kn_problem* kn) {
   if (!kn) return;
   KnImpl* im = static_cast<KnImpl*>(kn->impl);
   if (im) {
-    void* b[] = {im->in, im->sorted, im->cell_start, im->cell_fill, im->site_cell, im->scan_tmp, im->pos_of_id};
+    void* b[] = {im->in, im->sorted, im->cell_start, im->cell_fill, im->grid_work, im->scan_tmp, im->pos_of_id};
     for (void* p : b)
       if (p) cudaFree(p);
     delete im;
@@ -97,7 +97,7 @@ int kn_prepare_ex(kn_problem** out, const float* xyz, int n, int k) {
   };
   bool ok = A((void**)&im->in, sizeof(float4) * n) && A((void**)&im->sorted, sizeof(float4) * n) &&
             A((void**)&im->cell_start, sizeof(int) * (nc + 1)) && A((void**)&im->cell_fill, sizeof(int) * nc) &&
-            A((void**)&im->site_cell, sizeof(int) * n) &&
+            A((void**)&im->grid_work, sizeof(int) * grid_sort_work_ints(n, nc)) &&
             A((void**)&im->scan_tmp, sizeof(int) * scan_tmp_ints(nc + 1)) &&
             A((void**)&im->pos_of_id, sizeof(int) * n) &&
             A((void**)&kn->d_permutation, sizeof(unsigned) * n) && A((void**)&kn->d_counters, sizeof(int) * nc) &&
@@ -115,8 +115,7 @@ int kn_prepare_ex(kn_problem** out, const float* xyz, int n, int k) {
   }
   if (ce != cudaSuccess) { set_error("kn_prepare upload: %s", cudaGetErrorString(ce)); cudaFree(stage); kn_release(kn); return VGB_ERR_CUDA; }
   const ProbDesc lone = lone_problem(n, dim, 0, k);
-  int rc = grid_sort(im->in, im->sorted, n, nc, nullptr, nullptr, lone, im->cell_start, im->cell_fill, im->site_cell,
-                     im->scan_tmp, st);
+  int rc = grid_sort(im->in, im->sorted, n, nc, nullptr, nullptr, lone, im->cell_start, im->grid_work, st);
   if (!rc) {
     k_kn_views<<<(n + 255) / 256, 256, 0, st>>>(im->sorted, n, kn->d_stored_points, kn->d_permutation);
     k_kn_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(im->cell_start, (int)nc, kn->d_counters, kn->d_ptrs);

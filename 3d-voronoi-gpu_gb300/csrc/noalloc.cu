@@ -5,8 +5,8 @@
 // latency-critical loop where cudaMalloc's implicit synchronisation of the
 // device is not acceptable.  vgb_knn_noalloc serves them: the caller passes
 // device buffers for the points and the results, and every intermediate array
-// of the grid kNN (points with ids, their grid-ordered copy, cell ids, cell
-// starts and fill counters, the scan's tile sums, the id -> position map)
+// of the grid kNN (points with ids, their grid-ordered copy, cell starts, the
+// sort's keys, digit counts and scan tile sums, the id -> position map)
 // lives in one file-scope static device array, sized for at most
 // VGB_NOALLOC_MAX_POINTS points.  Every GPU that loads this library holds that
 // array (about 2.8 MB) until the process exits.
@@ -34,13 +34,10 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte offsets of the scratch arrays
 constexpr size_t OFF_IN = 0;
 constexpr size_t OFF_SORTED = OFF_IN + align256(sizeof(float4) * NA_MAX_POINTS);
-constexpr size_t OFF_SITE_CELL = OFF_SORTED + align256(sizeof(float4) * NA_MAX_POINTS);
-constexpr size_t OFF_POS_OF_ID = OFF_SITE_CELL + align256(sizeof(int) * NA_MAX_POINTS);
+constexpr size_t OFF_POS_OF_ID = OFF_SORTED + align256(sizeof(float4) * NA_MAX_POINTS);
 constexpr size_t OFF_CELL_START = OFF_POS_OF_ID + align256(sizeof(int) * NA_MAX_POINTS);
-constexpr size_t OFF_CELL_FILL = OFF_CELL_START + align256(sizeof(int) * (NA_MAX_CELLS + 1));
-constexpr size_t OFF_SCAN = OFF_CELL_FILL + align256(sizeof(int) * NA_MAX_CELLS);
-constexpr size_t SCAN_INTS = (NA_MAX_CELLS + 1 + 2047) / 2048 + 1;  // tiles of 2048 ints, plus the total
-constexpr size_t SCRATCH_BYTES = OFF_SCAN + align256(sizeof(int) * SCAN_INTS);
+constexpr size_t OFF_WORK = OFF_CELL_START + align256(sizeof(int) * (NA_MAX_CELLS + 1));
+constexpr size_t SCRATCH_BYTES = OFF_WORK + align256(sizeof(int) * grid_sort_work_ints(NA_MAX_POINTS, NA_MAX_CELLS));
 
 static __device__ __align__(256) unsigned char g_knn_scratch[SCRATCH_BYTES];
 
@@ -111,17 +108,14 @@ extern "C" int vgb_knn_noalloc(const float* d_points, int n, int k, unsigned* d_
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   float4* in = reinterpret_cast<float4*>(base + OFF_IN);
   float4* sorted = reinterpret_cast<float4*>(base + OFF_SORTED);
-  int* site_cell = reinterpret_cast<int*>(base + OFF_SITE_CELL);
   int* pos_of_id = reinterpret_cast<int*>(base + OFF_POS_OF_ID);
   int* cell_start = reinterpret_cast<int*>(base + OFF_CELL_START);
-  int* cell_fill = reinterpret_cast<int*>(base + OFF_CELL_FILL);
-  int* scan_tmp = reinterpret_cast<int*>(base + OFF_SCAN);
+  int* work = reinterpret_cast<int*>(base + OFF_WORK);
   k_na_pack<<<(n + 255) / 256, 256, 0, st>>>(d_points, n, in);
   VGB_CUDA_TRY(cudaGetLastError());
   // grid_sort clears the cell counters and fill counters it needs at zero
   const ProbDesc lone = lone_problem(n, dim, 0, k);
-  if (grid_sort(in, sorted, n, (long long)dim * dim * dim, nullptr, nullptr, lone, cell_start, cell_fill, site_cell,
-                scan_tmp, st))
+  if (grid_sort(in, sorted, n, (long long)dim * dim * dim, nullptr, nullptr, lone, cell_start, work, st))
     return VGB_ERR_CUDA;
   if (knn_sites(sorted, n, cell_start, nullptr, nullptr, lone, k, pos_of_id, d_knn, st)) return VGB_ERR_CUDA;
   k_na_perm<<<(n + 255) / 256, 256, 0, st>>>(sorted, n, d_perm);

@@ -142,11 +142,21 @@ int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t 
 
 // Grid sort of n sites (float4 x,y,z,id) by (cell, id); each site's cell is
 // its problem's cell_off + its cell in that problem's grid, so problems stay
-// in order and contiguous.
-//   cell_start: ncell + 1 ints; cell_fill, site_cell: scratch (ncell, n ints).
-//   scan_tmp: scan_tmp_ints(ncell + 1) ints.
+// in order and contiguous.  Stable radix sort of the sites in id order by
+// cell key; `in` is overwritten (scratch).
+//   cell_start: ncell + 1 ints; work: grid_sort_work_ints(n, ncell) ints.
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX_BUCKETS = 1 << RADIX_BITS;
+constexpr int RADIX_TILE = 2048;  // keys per warp tile
+constexpr long long grid_sort_tiles(long long n) { return (n + RADIX_TILE - 1) / RADIX_TILE; }
+constexpr size_t grid_sort_work_ints(long long n, long long ncell) {
+  // two key arrays, the digit counts, the scan scratch (tiles of 2048 ints)
+  return (size_t)(2 * n + RADIX_BUCKETS * grid_sort_tiles(n) +
+                  ((ncell + 1 > RADIX_BUCKETS * grid_sort_tiles(n) ? ncell + 1 : RADIX_BUCKETS * grid_sort_tiles(n)) +
+                   2047) / 2048 + 1);
+}
 int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int* cell_start, int* cell_fill, int* site_cell, int* scan_tmp, cudaStream_t st);
+              const ProbDesc& lone, int* cell_start, int* work, cudaStream_t st);
 
 // K nearest sorted sites of every sorted site (self excluded) or of every tet
 // centroid, ordered by (distance, id).  Output rows are sorted-space indices

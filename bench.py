@@ -2,15 +2,22 @@
 """Lloyd iterations per second of the clipped 3D Voronoi path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--method site_major|plain]
+                    [--workload NAME] [--method cell_tet|site_major|plain]
+                    [--reference-form] [--accuracy M] [--no-cpu-baseline]
 
 A step is one Lloyd iteration of the path over the whole site set: grid sort,
-site kNN, tet candidate sets, tet-cell clipping, per-site moments, update.
-The default workload is the voxelised torus (128^3 grid, 1,955,088 tets) with
-1,000,000 uniform sites, K = 64 (the reference's heuristic gives tet_k = 60).
-Inputs are generated (seeded) on the host, then resident in HBM; the working
-set (candidate lists, neighbour lists) is several times the 129 MB L2, so no
-flush is needed between steps.
+site kNN, per-tet reach, clipped cells (cell-tet method, exact form: cells
+inside the mesh whole, the others against every tet in reach), per-site
+moments, update.  --reference-form sums every cell over its tet_k candidate
+tets as the reference does; --method picks the tet-cell (site_major) or the
+thread-per-pair (plain) kernel instead.  The default workload is the voxelised
+torus (128^3 grid, 1,955,088 tets) with 1,000,000 uniform sites, K = 64 (the
+reference's heuristic gives tet_k = 60 for the reference form).  Inputs are
+generated (seeded) on the host, then resident in HBM; the working set
+(neighbour lists, tet records) is several times the 129 MB L2, so no flush is
+needed between steps.  --workload batch256_kuhn runs the batched form (256
+independent problems per launch).  --accuracy M adds the per-iteration error
+of M sampled cells against the FP64 oracle.
 
 Printed (rank 0, one JSON line): value = Lloyd iter/s with inputs resident
 (CUDA events on the engine stream around exactly K steps, after W warm-up
@@ -66,10 +73,24 @@ WORKLOADS = {
     "batch256_kuhn": dict(kind="batch", n_prob=256, K=0,
                           desc="256 independent Kuhn cubes, side n uniform in [4,48], interior jitter 0.1 spacing; "
                                "sites log-uniform in [500, 200000] per problem, uniform in the cube; K autotuned "
-                               "in {32,48,64,96} per problem, grid density autotuned"),
+                               "in {32,48,64,96,128} per problem, grid density autotuned"),
 }
 DEFAULT_WORKLOAD = "torus128_uniform_1m"
-LAUNCHES_PER_STEP = {"cell_tet": 16, "site_major": 16, "plain": 11}
+# kernels per step besides the grid sort: kNN 2, then exact form: reach, clip,
+# update; reference form: candidate kNN, candidate lists (count, scan x3,
+# fill), clip, update; plain: candidate kNN, clip, update
+LAUNCHES_PER_STEP = {"exact": 5, "cell_tet": 10, "site_major": 10, "plain": 5}
+
+
+def grid_sort_launches(ncell: int) -> int:
+    """Gather + cell-count scan (3), then per 8-bit digit of the cell key a
+    histogram, a scan (3) and a scatter."""
+    passes = 0
+    top = max(ncell - 1, 0)
+    while top > 0:
+        passes += 1
+        top >>= 8
+    return 4 + 5 * passes
 
 # algorithmic FP32 work of the clip kernel, per counted event (see DESIGN.md)
 FLOPS_CONFLICT = 7      # plane test of one cell vertex: 3 FMA + compare
@@ -372,6 +393,10 @@ def run_ours(args):
                     "peak_source": f"{peak_src} hbm_gbs", "bytes_per_launch": knn_bytes,
                     "ms_per_launch": round(phases["knn"], 4)}
 
+    accuracy = None
+    if args.accuracy > 0 and rank == 0:
+        accuracy = accuracy_run(eng, P, K, args.accuracy, args.accuracy_iters)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         checker = load_checker()
@@ -407,7 +432,8 @@ def run_ours(args):
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
                    "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
                    "parallelism": f"replicas x{world}"},
-        "gpu_launches": (11 if exact else LAUNCHES_PER_STEP[args.method]) * args.steps,
+        "gpu_launches": (LAUNCHES_PER_STEP["exact" if exact else args.method] +
+                         grid_sort_launches(eng.grid_dim ** 3)) * args.steps,
         "e2e": e2e,
         "roofline": roofline,
         "roofline_knn": roofline_knn,
@@ -418,7 +444,48 @@ def run_ours(args):
         "clocks": clk,
         "cpu_baseline": cpu,
     }
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     print(json.dumps(line), flush=True)
+
+
+def accuracy_run(eng, P, K, m, iters):
+    """Per-iteration error of the cells against the FP64 oracle: before each
+    Lloyd iteration the positions are saved; the iteration's moments (of those
+    positions) are compared, for m sampled sites, with the oracle's clipped
+    cells (every tet within twice the K-th neighbour distance), and the total
+    volume of all cells with the mesh volume."""
+    checker = load_checker()
+    mesh_vol = checker.mesh_volume(P.verts, P.tets)
+    lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
+    diag = float(np.linalg.norm(hi - lo))
+    rng = np.random.default_rng(7)
+    out = []
+    for it in range(iters):
+        xyz0, ids0 = eng.sites()
+        pre = np.empty_like(xyz0)
+        pre[ids0] = xyz0
+        eng.iterate(1, update=True)
+        eng.sync()
+        vol, mom = eng.moments()
+        _, ids = eng.sites()
+        knn = eng.buffer("knn").astype(np.int64)
+        pos = pre[ids]                                  # pre-update positions, this iteration's grid order
+        smp = rng.choice(len(pos), m, replace=False)
+        dK = np.linalg.norm(pos[knn[smp, K - 1]] - pos[smp], axis=1)
+        r = checker.sample_cells(pos, smp, knn[smp], P.verts, P.tets, 2.0 * dK + 1.0)
+        ok = r["vol"] > 0
+        vrel = np.abs(vol[smp][ok] - r["vol"][ok]) / r["vol"][ok]
+        b_gpu = mom[smp][ok] / vol[smp][ok, None]
+        b_orc = r["mom"][ok] / r["vol"][ok, None]
+        brel = np.linalg.norm(b_gpu - b_orc, axis=1) / diag
+        out.append({"iteration": it + 1, "sampled": int(ok.sum()), "vol_rel_max": float(vrel.max()),
+                    "vol_rel_p99": float(np.percentile(vrel, 99)), "bary_diag_max": float(brel.max()),
+                    "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol)})
+    worst = {k: max(o[k] for o in out) for k in ("vol_rel_max", "bary_diag_max", "total_vol_rel")}
+    return {"oracle": "FP64 cell-tet restatement (oracle/), per sampled site, every tet in reach",
+            "sample_per_iteration": m, "iterations": out, "worst": worst,
+            "bars": {"vol_rel": 1e-5, "bary_diag": 1e-6, "total_vol_rel": 1e-6}}
 
 
 def run_batch(args):
@@ -457,6 +524,7 @@ def run_batch(args):
     stats = B.stats()
     ks = collections.Counter(B.problem(p)["site_k"] for p in range(B.n_prob))
     n_site, n_tet, n_prob, dens = B.n_site, B.n_tet, B.n_prob, B.density
+    n_cells = sum(B.problem(p)["grid_dim"] ** 3 for p in range(n_prob))
     B.close()
     if rank != 0:
         return
@@ -469,7 +537,7 @@ def run_batch(args):
                    "grid_density": round(dens, 2), "form": "exact, batched (one launch per kernel per iteration)",
                    "cuda_graph": True, "create_s": round(create_s, 2), "l2": "inputs larger than L2, no flush",
                    "parallelism": f"replicas x{world}"},
-        "gpu_launches": 11 * args.steps,
+        "gpu_launches": (LAUNCHES_PER_STEP["exact"] + grid_sort_launches(n_cells)) * args.steps,
         "e2e": None,
         "sites_per_s": round(n_site * value / world, 1),
         "stats": stats,
@@ -560,6 +628,9 @@ def main():
                     help="cell-tet: sum every cell over its tet_k candidate tets, as the reference does, instead "
                          "of the exact form (cells inside the mesh whole, the rest against every tet in reach)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy", type=int, default=0, metavar="M",
+                    help="after timing, report per-iteration error against the FP64 oracle on M sampled sites")
+    ap.add_argument("--accuracy-iters", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

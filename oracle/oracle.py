@@ -166,6 +166,36 @@ def cell_tet(sites, nbr, verts, tets, cand, mode: int = FIXED, nthreads: int = 0
     return dict(vol=vol, mom=mom, hist=hist)
 
 
+def sample_cells(sites, sample, nbr, verts, tets, reach, mode: int = FIXED, nthreads: int = 0):
+    """Moments of the clipped cells of a sample of the sites, every tet in
+    reach (the cell-tet method of voronoi.cu:620-660, 703-726, per pair).
+
+    sites: (n,3) all sites; sample: (m,) indices of the sites to evaluate;
+    nbr: (m,K) their neighbour lists (indices into sites); reach: (m,) a
+    radius around each sampled site that holds its whole cell.  A tet is a
+    candidate of site i when its centroid lies within reach[i] plus its own
+    bounding radius; each (tet, site) pair becomes a row of one candidate.
+    Returns dict(vol (m,), mom (m,3)) in FP64 (mode FIXED)."""
+    from scipy.spatial import cKDTree
+    sites, verts, tets = _f32(sites), _f32(verts), _i32(tets)
+    sample = np.asarray(sample, np.int64)
+    n, m = len(sites), len(sample)
+    order = np.concatenate([sample, np.setdiff1d(np.arange(n), sample)])
+    pos = np.empty(n, np.int64)
+    pos[order] = np.arange(n)
+    s2 = sites[order]
+    nbr2 = pos[np.asarray(nbr, np.int64)].astype(np.int32)
+    corners = verts[tets]                                   # (nt, 4, 3)
+    cent = corners.mean(axis=1)
+    rt = np.sqrt(((corners - cent[:, None, :]) ** 2).sum(-1)).max(1)
+    tree = cKDTree(cent)
+    hits = tree.query_ball_point(s2[:m], np.asarray(reach, np.float64) + float(rt.max()) * 1.001 + 1e-3)
+    pt = np.concatenate([np.asarray(h, np.int64) for h in hits]) if m else np.zeros(0, np.int64)
+    ps = np.repeat(np.arange(m), [len(h) for h in hits]).astype(np.int32)
+    r = cell_tet(s2, nbr2, verts, tets[pt], ps.reshape(-1, 1), mode=mode, nthreads=nthreads)
+    return dict(vol=r["vol"], mom=r["mom"], pairs=len(pt))
+
+
 def lloyd_update(sites, vol, mom, mode: int = FIXED):
     s = _f32(sites).copy()
     lib().orc_lloyd_update(mode, _p(s), len(s), _p(np.ascontiguousarray(vol, np.float64)),
