@@ -9,7 +9,7 @@
 // sort's keys, digit counts and scan tile sums, the id -> position map)
 // lives in one file-scope static device array, sized for at most
 // VGB_NOALLOC_MAX_POINTS points.  Every GPU that loads this library holds that
-// array (about 2.8 MB) until the process exits.
+// array (about 2.9 MB) until the process exits.
 //
 // Host code never dereferences the array's name: on the host it is only a
 // stand-in, not a device address.  The first call on each device (with that

@@ -191,7 +191,7 @@ int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const int* indic
  * d_knn (n x k) holds the k nearest points of each point in grid order, as
  * grid positions, and d_perm (n) maps grid position -> input index.  All
  * pointers are device memory owned by the caller; d_points is n x 3 floats.
- * Intermediate arrays live in one static device array of about 2.8 MB, held
+ * Intermediate arrays live in one static device array of about 2.9 MB, held
  * by every GPU that loads the library until the process exits, so n is at
  * most VGB_NOALLOC_MAX_POINTS (larger n returns VGB_ERR_INVALID) and
  * 1 <= k <= 128, k < n.  Work is queued on `stream` (a cudaStream_t, NULL for
