@@ -307,8 +307,9 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (!verts || !tets || !sites || n_vert <= 0 || n_tet <= 0 || n_site <= 1) {
     set_error("empty mesh or fewer than two sites"); return VGB_ERR_INVALID;
   }
-  if (cfg.site_k <= 0 || cfg.site_k > MAX_SITE_K || cfg.site_k >= n_site) {
-    set_error("site_k=%d must be in [1, min(%d, n_site-1)]", cfg.site_k, MAX_SITE_K); return VGB_ERR_INVALID;
+  if (cfg.site_k < 0 || cfg.site_k > MAX_SITE_K || cfg.site_k >= n_site) {
+    set_error("site_k=%d must be 0 (autotune) or in [1, min(%d, n_site-1)]", cfg.site_k, MAX_SITE_K);
+    return VGB_ERR_INVALID;
   }
   if (cfg.method != VGB_METHOD_SITE_MAJOR && cfg.method != VGB_METHOD_PLAIN && cfg.method != VGB_METHOD_CELL_TET) {
     set_error("unknown method %d", cfg.method); return VGB_ERR_INVALID;
@@ -319,7 +320,9 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   if (!e) { set_error("host allocation failed"); return VGB_ERR_NOMEM; }
   e->cfg = cfg;
   e->n_vert = n_vert; e->n_tet = n_tet; e->n = n_site;
-  e->K = cfg.site_k;
+  // site_k 0: autotuned after the upload; buffers sized for the largest K
+  const int k_cap = std::min(MAX_SITE_K, n_site - 1);
+  e->K = cfg.site_k > 0 ? cfg.site_k : k_cap;
   e->tk = vgb_tet_k(n_site, n_tet, cfg.tet_k);
   if (e->tk > MAX_TET_K) { set_error("tet_k=%d above %d", e->tk, MAX_TET_K); delete e; return VGB_ERR_INVALID; }
   e->dim = cfg.grid_dim > 0 ? cfg.grid_dim : vgb_grid_dim(n_site);
@@ -427,6 +430,18 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   }
   if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
+  if (cfg.site_k == 0) {
+    // K: the smallest of 32, 48, 64, 96, 128 (at most n - 1) whose cells all
+    // reach the security radius -- more neighbours cannot change such a cell
+    static const int cand[] = {32, 48, 64, 96, MAX_SITE_K};
+    for (int k : cand) {
+      e->K = e->prob.K = std::min(k, k_cap);
+      unsigned long long st[VGB_STAT_COUNT];
+      if ((rc = run_pass(e, 0)) || (rc = vgb_engine_get_stats(e, st))) { free_engine(e); return rc; }
+      if (st[VGB_STAT_SECURITY_MISS] == 0 || e->K == k_cap) break;
+    }
+    if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
+  }
   *out = e;
   return VGB_OK;
 }

@@ -120,10 +120,55 @@ def kuhn_grid(cells: np.ndarray, n: int):
 
 def kuhn_cube(n: int):
     """Unit cube split into n^3 cubes, 6 Kuhn tets each: 6 n^3 tets, (n+1)^3 vertices."""
+    if n > 64:
+        return kuhn_cube_large(n)
     g = np.arange(n)
     cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
     _, pos, tets = kuhn_grid(cells, n)
     return pos, tets
+
+
+def kuhn_cube_large(n: int):
+    """kuhn_cube for large n without the vertex de-duplication: every lattice
+    vertex is used, so tets index the (n+1)^3 lattice directly, int32; each of
+    the six Kuhn types has one orientation, fixed once."""
+    n1 = n + 1
+    off = _corner_offsets()
+    corner_id = off[:, 0] + n1 * (off[:, 1] + n1 * off[:, 2])          # (8,)
+    local = corner_id[_KUHN]                                            # (6, 4)
+    unit = off.astype(np.float64)
+    for t in range(6):
+        if orient(unit, _KUHN[t:t + 1])[0] < 0:
+            local[t] = local[t][[0, 1, 3, 2]]
+    g = np.arange(n, dtype=np.int64)
+    base = (g[:, None, None] + n1 * (g[None, :, None] + n1 * g[None, None, :])).transpose(2, 1, 0).ravel()
+    tets = np.empty((n ** 3 * 6, 4), np.int32)
+    step = 1 << 20
+    for a in range(0, len(base), step):
+        b = base[a:a + step]
+        tets[6 * a:6 * (a + len(b))] = (b[:, None, None] + local[None, :, :]).reshape(-1, 4)
+    ax = np.arange(n1, dtype=np.float32) / np.float32(n)
+    pos = np.empty((n1 ** 3, 3), np.float32)
+    pos[:, 0] = np.tile(ax, n1 * n1)
+    pos[:, 1] = np.tile(np.repeat(ax, n1), n1)
+    pos[:, 2] = np.repeat(ax, n1 * n1)
+    return pos, tets
+
+
+def gradient_sites(n: int, rng, ratio: float = 4.0) -> np.ndarray:
+    """n sites in [0,1]^3, density rising linearly along x from 1 to `ratio`."""
+    a = ratio - 1.0
+    u = rng.uniform(0.0, 1.0, n)
+    x = (-1.0 + np.sqrt(1.0 + 2.0 * a * u * (1.0 + a / 2.0))) / a   # inverse CDF of (1 + a x) / (1 + a/2)
+    return np.stack([x, rng.uniform(0.0, 1.0, n), rng.uniform(0.0, 1.0, n)], axis=1)
+
+
+def large_problem(n_cells: int = 256, n_site: int = 8_000_000, seed: int = 1) -> Problem:
+    """Unit cube as an n_cells^3 Kuhn grid, sites with a 4:1 density gradient along x."""
+    pos, tets = kuhn_cube(n_cells)
+    rng = np.random.default_rng(seed)
+    v, s = normalize(pos, gradient_sites(n_site, rng))
+    return Problem(f"kuhn{n_cells}_grad_s{n_site}", v, tets, s)
 
 
 def _jitter(pos: np.ndarray, tets: np.ndarray, movable: np.ndarray, amount: float, rng) -> np.ndarray:

@@ -69,6 +69,10 @@ WORKLOADS = {
     # the small configuration
     "kuhn20_20k": dict(kind="cube", cells=20, n=20000, K=64,
                        desc="unit cube, 20^3 Kuhn grid (48,000 tets); 20,000 uniform sites; K=64"),
+    # the large configuration: one big cube, density gradient, K autotuned
+    "kuhn256_grad_8m": dict(kind="large", cells=256, n=8_000_000, K=0,
+                            desc="unit cube as a 256^3 Kuhn grid (100,663,296 tets); 8,000,000 sites with a 4:1 "
+                                 "density gradient along x; K autotuned in {32,48,64,96,128}"),
     # the batched configuration: many independent problems per launch
     "batch256_kuhn": dict(kind="batch", n_prob=256, K=0,
                           desc="256 independent Kuhn cubes, side n uniform in [4,48], interior jitter 0.1 spacing; "
@@ -120,6 +124,8 @@ def make_problem(name: str):
     w = WORKLOADS[name]
     if w["kind"] == "torus":
         return mg.torus_problem(w["n"], grid=w["grid"], sites=w["sites"], seed=1)
+    if w["kind"] == "large":
+        return mg.large_problem(w["cells"], w["n"], seed=1)
     return mg.cube_problem(w["cells"], w["n"], seed=1)
 
 
@@ -319,6 +325,7 @@ def run_ours(args):
     exact = args.method == "cell_tet" and not args.reference_form
     eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
                      exact=exact)
+    K = eng.site_k  # the autotuned K when the workload asks for one
 
     def barrier():
         if dist:
@@ -453,8 +460,9 @@ def accuracy_run(eng, P, K, m, iters):
     """Per-iteration error of the cells against the FP64 oracle: before each
     Lloyd iteration the positions are saved; the iteration's moments (of those
     positions) are compared, for m sampled sites, with the oracle's clipped
-    cells (every tet within twice the K-th neighbour distance), and the total
-    volume of all cells with the mesh volume."""
+    cells (every tet within the K-th neighbour distance: twice the bound on a
+    cell that reaches its security radius), and the total volume of all cells
+    with the mesh volume."""
     checker = load_checker()
     mesh_vol = checker.mesh_volume(P.verts, P.tets)
     lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
@@ -473,15 +481,19 @@ def accuracy_run(eng, P, K, m, iters):
         pos = pre[ids]                                  # pre-update positions, this iteration's grid order
         smp = rng.choice(len(pos), m, replace=False)
         dK = np.linalg.norm(pos[knn[smp, K - 1]] - pos[smp], axis=1)
-        r = checker.sample_cells(pos, smp, knn[smp], P.verts, P.tets, 2.0 * dK + 1.0)
+        r = checker.sample_cells(pos, smp, knn[smp], P.verts, P.tets, dK + 1.0)
         ok = r["vol"] > 0
         vrel = np.abs(vol[smp][ok] - r["vol"][ok]) / r["vol"][ok]
         b_gpu = mom[smp][ok] / vol[smp][ok, None]
         b_orc = r["mom"][ok] / r["vol"][ok, None]
         brel = np.linalg.norm(b_gpu - b_orc, axis=1) / diag
+        w = int(np.argmax(vrel))
+        sw = smp[ok][w]
         out.append({"iteration": it + 1, "sampled": int(ok.sum()), "vol_rel_max": float(vrel.max()),
                     "vol_rel_p99": float(np.percentile(vrel, 99)), "bary_diag_max": float(brel.max()),
-                    "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol)})
+                    "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol),
+                    "worst_cell": {"site": pos[sw].tolist(), "vol": float(vol[sw]), "oracle_vol": float(r["vol"][ok][w]),
+                                   "kth_neighbour_dist": float(dK[ok][w])}})
     worst = {k: max(o[k] for o in out) for k in ("vol_rel_max", "bary_diag_max", "total_vol_rel")}
     return {"oracle": "FP64 cell-tet restatement (oracle/), per sampled site, every tet in reach",
             "sample_per_iteration": m, "iterations": out, "worst": worst,

@@ -81,7 +81,9 @@ enum vgb_buffer {
 };
 
 typedef struct vgb_config {
-  int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9)   */
+  int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9);
+                   0 = autotune: the smallest of 32, 48, 64, 96, 128 whose cells all
+                   reach the security radius on the initial sites                    */
   int tet_k;    /* candidate sites per tet; 0 = the reference heuristic (voronoi.cu:936) */
   int grid_dim; /* site grid side; 0 = round((n/3.1)^(1/3)) (knearests.cu:243)           */
   int method;   /* VGB_METHOD_*                                                          */

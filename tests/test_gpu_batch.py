@@ -99,3 +99,18 @@ def test_batch_invalid(pkg, meshgen):
     bad[0, 0] = len(P.verts)
     with pytest.raises(pkg.VoronoiError):
         pkg.Batch([(P.verts, bad, P.sites)], site_k=16, tune_grid=False)
+
+
+def test_lone_engine_autotunes_k(pkg, meshgen):
+    """site_k=0 on a lone engine: the smallest candidate K with no security
+    miss (the batch rule), and the same K as a batch of that one problem."""
+    P = meshgen.cube_problem(9, 3000, seed=2, jitter=0.1)
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=0, exact=True) as E:
+        K = E.site_k
+        assert K in (32, 48, 64, 96, 128)
+        E.iterate(1, update=False)
+        E.sync()
+        if K < 128:
+            assert E.stats()["security_miss"] == 0
+    with pkg.Batch([(P.verts, P.tets, P.sites)], site_k=0, tune_grid=False) as B:
+        assert B.problem(0)["site_k"] == K
