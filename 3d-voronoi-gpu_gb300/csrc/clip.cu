@@ -346,19 +346,28 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
       const int pend = job == 1 ? pbeg + BOX_PLANES : bis ? 4 + K : 4;
       int state = 0;  // 0 kept, 1 empty, 2 dropped
       bool secmiss = bis;
+      // counters of the sequence, packed: planes (bits 0-7), cuts (8-15),
+      // vertex-vs-plane tests (16-31); at most 138 planes of 128 vertices
+      unsigned seq_cnt = 0u;
+      const bool need_r2 = job != 2 || !CELL_TET;
       for (int pi = pbeg; pi < pend; ++pi) {
         const float4 P = S.plane[pi];
-        if (lane == 0) { S.cnt[WC_PLANES]++; S.cnt[WC_CONFLICT] += (unsigned)c.nt; }
-        const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane);
+        seq_cnt += 1u + ((unsigned)c.nt << 16);
+        const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane, need_r2);
         if (r == CLIP_EMPTY) { state = 1; break; }
         if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
           if (lane == 0) S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
           state = 2;
           break;
         }
-        if (r == CLIP_CUT && lane == 0) S.cnt[WC_CLIPS]++;
+        if (r == CLIP_CUT) seq_cnt += 1u << 8;
         // |neighbour - site|^2 > 4 max|v - site|^2
         if (bis && 2.f * P.w > 4.f * c.r2) { secmiss = false; break; }
+      }
+      if (lane == 0) {
+        S.cnt[WC_PLANES] += seq_cnt & 0xffu;
+        S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
+        S.cnt[WC_CONFLICT] += seq_cnt >> 16;
       }
       if (job == 2 && bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
 

@@ -104,9 +104,10 @@ __device__ __forceinline__ void cell_clear(WarpCell& c) {
 // boundary edge, else the cell is dropped (the reference's
 // inconsistent_boundary).  New triangles fill freed slots; the receiving lane
 // computes the new vertex.  conf and bedge are MAX_TRI-entry scratch arrays of
-// the warp.
+// the warp.  need_r2: keep c.r2 (the largest |vertex|^2) current; callers that
+// never read it skip the warp reduction.
 __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsigned pidx, const float4* planes,
-                                         unsigned* conf, unsigned* bedge, const int lane) {
+                                         unsigned* conf, unsigned* bedge, const int lane, const bool need_r2) {
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   unsigned m[TRI_SLOTS];
   int nconf = 0;
@@ -237,7 +238,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
   // inconsistent (a plane through an edge, within rounding); drop the cell
   if (__any_sync(FULL, nonfinite)) return CLIP_BOUNDARY;
   c.nt = nt2;
-  c.r2 = warp_max(lm);
+  if (need_r2) c.r2 = warp_max(lm);
   __syncwarp();
   return CLIP_CUT;
 }
