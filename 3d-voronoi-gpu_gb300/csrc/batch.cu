@@ -382,6 +382,12 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     if (ce == cudaSuccess) ce = cudaMemcpy(b->field_sat, sat.data(), sizeof(unsigned) * sat.size(), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemset(b->mom, 0, sizeof(dmom4) * (size_t)b->n);
     if (ce != cudaSuccess) { set_error("batch upload: %s", cudaGetErrorString(ce)); free_batch(b); return VGB_ERR_CUDA; }
+    for (int p = 0; p < n_prob; ++p)
+      if (field_clear_radius(b->field + b->probs[p].field_off, b->field_sat + b->probs[p].sat_off, b->probs[p].fdim,
+                             b->st)) {
+        free_batch(b);
+        return VGB_ERR_CUDA;
+      }
   }
   if ((rc = layout(b))) { free_batch(b); return rc; }
   if (cfg.site_k == 0) {

@@ -73,6 +73,24 @@ struct SiteSmem {
   float mr2;
 };
 
+// The site's cell into its shared copy, which the box bound and every tet
+// clip start from.
+__device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int lane) {
+  const unsigned lane_bit = 1u << lane;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k)
+    if (c.vm[k] & lane_bit) {
+      S.mtri[k * WARP + lane] = c.tri[k];
+      S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
+    }
+  if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
+  if (lane == 0) {
+    S.mnt = c.nt;
+    S.mr2 = c.r2;
+  }
+  __syncwarp();
+}
+
 // One kernel body, one copy of the clip and of the moments: every cell of a
 // site -- the cell built from the bisectors (cell-tet method) and each
 // candidate tet's cell -- goes through the same plane loop and the same
@@ -375,16 +393,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
       bool take = state == 0, interior = false;
       if (job == 0) {
         if (state != 0) break;  // the site's cell failed: no tet is clipped
-#pragma unroll
-        for (int k = 0; k < TRI_SLOTS; ++k)
-          if (c.vm[k] & lane_bit) {
-            S.mtri[k * WARP + lane] = c.tri[k];
-            S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
-          }
-        if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
-        if (lane == 0) { S.mnt = c.nt; S.mr2 = c.r2; }
-        __syncwarp();
         if (secmiss) {
+          // the box bound and the tets start from the cell's shared copy
+          store_master(c, S, lane);
           job = 1;
           continue;
         }
@@ -424,21 +435,32 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         // inside the domain box, so the bound above left the cell as built).
         const float Rq = Rc * 1.001f + 0.01f;
         const int fdim = field ? PD(fdim) : 1;
-        if (field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
-            seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f &&
-            field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]) {
+        const int fv = field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
+                               seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f
+                           ? field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]
+                           : 0;
+        if (fv) {
+          // field value = 1 + the cell's clear radius (cells to the nearest
+          // touched one); beyond it, the summed table decides
+          const int ci = grid_axis(seed.x, fdim), cj = grid_axis(seed.y, fdim), ck = grid_axis(seed.z, fdim);
           const int a0 = grid_axis(seed.x - Rq, fdim), a1 = grid_axis(seed.x + Rq, fdim) + 1;
           const int b0 = grid_axis(seed.y - Rq, fdim), b1 = grid_axis(seed.y + Rq, fdim) + 1;
           const int c0 = grid_axis(seed.z - Rq, fdim), c1 = grid_axis(seed.z + Rq, fdim) + 1;
-          const size_t W = (size_t)fdim + 1;
-          const unsigned* sat = field_sat + PD(sat_off);
-          auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
-          const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
-                                   at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
-          interior = touched == 0u;
+          const int need = max(max(max(ci - a0, a1 - 1 - ci), max(cj - b0, b1 - 1 - cj)), max(ck - c0, c1 - 1 - ck));
+          if (need < fv) {
+            interior = true;
+          } else {
+            const size_t W = (size_t)fdim + 1;
+            const unsigned* sat = field_sat + PD(sat_off);
+            auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
+            const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
+                                     at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
+            interior = touched == 0u;
+          }
         }
         take = interior;
         if (!interior) {
+          if (!build_miss) store_master(c, S, lane);
           // the planes that bound the cell (ids present in its triangles)
           unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
 #pragma unroll
@@ -558,6 +580,36 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                                                                     tets, site_start, site_tets, mom, stats, nullptr,
                                                                     nullptr, nullptr, nullptr, nullptr, nullptr,
                                                                     nullptr, prob_secmiss);
+  VGB_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// Clear radius of the inside field: an inside cell's byte becomes 1 + the
+// largest r (at most 254) such that the cube of cells [c - r, c + r]^3 lies in
+// the grid and holds no cell touched by the mesh boundary (binary search on
+// the summed table).  Once per mesh.
+__global__ void k_field_clear(unsigned char* __restrict__ field, const unsigned* __restrict__ sat, int fdim) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nc = (long long)fdim * fdim * fdim;
+  if (c >= nc || !field[c]) return;
+  const int i = (int)(c % fdim), j = (int)((c / fdim) % fdim), k = (int)(c / ((long long)fdim * fdim));
+  const size_t W = (size_t)fdim + 1;
+  auto at = [&](int x, int y, int z) { return sat[(size_t)x + W * ((size_t)y + W * (size_t)z)]; };
+  int lo = 0, hi = min(254, min(min(min(i, j), k), min(min(fdim - 1 - i, fdim - 1 - j), fdim - 1 - k)));
+  while (lo < hi) {
+    const int r = (lo + hi + 1) >> 1;
+    const int x0 = i - r, x1 = i + r + 1, y0 = j - r, y1 = j + r + 1, z0 = k - r, z1 = k + r + 1;
+    const unsigned t = at(x1, y1, z1) - at(x0, y1, z1) - at(x1, y0, z1) - at(x1, y1, z0) + at(x0, y0, z1) +
+                       at(x0, y1, z0) + at(x1, y0, z0) - at(x0, y0, z0);
+    if (t == 0u) lo = r; else hi = r - 1;
+  }
+  field[c] = (unsigned char)(1 + lo);
+}
+
+int field_clear_radius(unsigned char* field, const unsigned* sat, int fdim, cudaStream_t st) {
+  const long long nc = (long long)fdim * fdim * fdim;
+  if (nc <= 0) return 0;
+  k_field_clear<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(field, sat, fdim);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -428,6 +428,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     if (ce == cudaSuccess)
       ce = cudaMemcpy(e->field_sat, field_sat.data(), sizeof(unsigned) * field_sat.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { set_error("field upload: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
+    if (field_clear_radius(e->field, e->field_sat, e->fdim, e->st)) { free_engine(e); return VGB_ERR_CUDA; }
   }
   if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
   if (cfg.site_k == 0) {

@@ -210,6 +210,10 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.
 
+// Inside field of one problem: turn the inside flags (fdim^3 bytes) into
+// 1 + the clear radius in cells, from the summed table of touched cells.
+int field_clear_radius(unsigned char* field, const unsigned* sat, int fdim, cudaStream_t st);
+
 // Absolute moments and the Lloyd update of n sites (engine.cu).
 int finish_sites(float4* sites, int n, dmom4* mom, int update, cudaStream_t st);
 
