@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
           }
           c.vm[0] = 0xfu;
           c.nt = 4;
-          c.r2 = warp_max(lane < 4 ? c.vw[0] : 0.f);
+          c.r2 = warp_max_nonneg(lane < 4 ? c.vw[0] : 0.f);
         }
         __syncwarp();
       }

@@ -61,6 +61,11 @@ __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
   return v;
 }
+// Largest of one non-negative float per lane: their bits order as unsigned
+// integers, so one warp reduction does it.
+__device__ __forceinline__ float warp_max_nonneg(float v) {
+  return __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(v)));
+}
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
@@ -238,7 +243,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
   // inconsistent (a plane through an edge, within rounding); drop the cell
   if (__any_sync(FULL, nonfinite)) return CLIP_BOUNDARY;
   c.nt = nt2;
-  if (need_r2) c.r2 = warp_max(lm);
+  if (need_r2) c.r2 = warp_max_nonneg(lm);
   __syncwarp();
   return CLIP_CUT;
 }
