@@ -73,6 +73,33 @@ struct SiteSmem {
   float mr2;
 };
 
+// Bounding box of the cell's vertices (site-relative), over the warp: float
+// bits mapped to an order-preserving unsigned key for the integer reductions.
+__device__ __forceinline__ unsigned ord_key(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_val(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ void cell_bounds(const WarpCell& c, int lane, float lo[3], float hi[3]) {
+  const unsigned lane_bit = 1u << lane;
+  float l0 = FLT_MAX, l1 = FLT_MAX, l2 = FLT_MAX, h0 = -FLT_MAX, h1 = -FLT_MAX, h2 = -FLT_MAX;
+#pragma unroll
+  for (int k = 0; k < TRI_SLOTS; ++k)
+    if (c.vm[k] & lane_bit) {
+      l0 = fminf(l0, c.vx[k]); h0 = fmaxf(h0, c.vx[k]);
+      l1 = fminf(l1, c.vy[k]); h1 = fmaxf(h1, c.vy[k]);
+      l2 = fminf(l2, c.vz[k]); h2 = fmaxf(h2, c.vz[k]);
+    }
+  lo[0] = ord_val(__reduce_min_sync(FULL, ord_key(l0)));
+  lo[1] = ord_val(__reduce_min_sync(FULL, ord_key(l1)));
+  lo[2] = ord_val(__reduce_min_sync(FULL, ord_key(l2)));
+  hi[0] = ord_val(__reduce_max_sync(FULL, ord_key(h0)));
+  hi[1] = ord_val(__reduce_max_sync(FULL, ord_key(h1)));
+  hi[2] = ord_val(__reduce_max_sync(FULL, ord_key(h2)));
+}
+
 // The site's cell into its shared copy, which the box bound and every tet
 // clip start from.
 __device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int lane) {
@@ -429,33 +456,46 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
         Rc = sqrtf(c.r2);
         // A cell that provably lies inside the mesh is its own clipped cell:
         // the sum over the tets it meets of (cell ^ tet) is the cell itself.
-        // The cell lies within Rc of its site; when the box of field cells
-        // covering that ball holds no cell touched by the mesh boundary and
-        // the site's field cell is inside, the ball is inside the mesh (and
-        // inside the domain box, so the bound above left the cell as built).
+        // When the box of field cells covering the cell holds no cell touched
+        // by the mesh boundary and the site's field cell is inside, the cell
+        // is inside the mesh (and inside the domain box, so the bound above
+        // left it as built).  First the ball of radius Rc against the site
+        // cell's clear radius (one byte), then the cell's vertex bounding box
+        // against the summed table.
         const float Rq = Rc * 1.001f + 0.01f;
         const int fdim = field ? PD(fdim) : 1;
-        const int fv = field && !secmiss && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f &&
-                               seed.y + Rq <= 1000.f && seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f
+        const int fv = field && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
+                               seed.y <= 1000.f && seed.z >= 0.f && seed.z <= 1000.f
                            ? field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]
                            : 0;
         if (fv) {
           // field value = 1 + the cell's clear radius (cells to the nearest
-          // touched one); beyond it, the summed table decides
-          const int ci = grid_axis(seed.x, fdim), cj = grid_axis(seed.y, fdim), ck = grid_axis(seed.z, fdim);
-          const int a0 = grid_axis(seed.x - Rq, fdim), a1 = grid_axis(seed.x + Rq, fdim) + 1;
-          const int b0 = grid_axis(seed.y - Rq, fdim), b1 = grid_axis(seed.y + Rq, fdim) + 1;
-          const int c0 = grid_axis(seed.z - Rq, fdim), c1 = grid_axis(seed.z + Rq, fdim) + 1;
-          const int need = max(max(max(ci - a0, a1 - 1 - ci), max(cj - b0, b1 - 1 - cj)), max(ck - c0, c1 - 1 - ck));
-          if (need < fv) {
-            interior = true;
-          } else {
-            const size_t W = (size_t)fdim + 1;
-            const unsigned* sat = field_sat + PD(sat_off);
-            auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
-            const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
-                                     at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
-            interior = touched == 0u;
+          // touched one)
+          if (seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f && seed.y + Rq <= 1000.f &&
+              seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f) {
+            const int ci = grid_axis(seed.x, fdim), cj = grid_axis(seed.y, fdim), ck = grid_axis(seed.z, fdim);
+            const int need = max(max(max(ci - grid_axis(seed.x - Rq, fdim), grid_axis(seed.x + Rq, fdim) - ci),
+                                     max(cj - grid_axis(seed.y - Rq, fdim), grid_axis(seed.y + Rq, fdim) - cj)),
+                                 max(ck - grid_axis(seed.z - Rq, fdim), grid_axis(seed.z + Rq, fdim) - ck));
+            interior = need < fv;
+          }
+          if (!interior) {
+            float lo[3], hi[3];
+            cell_bounds(c, lane, lo, hi);
+            const float m = 1e-3f * Rc + 0.01f;
+            const float x0 = seed.x + lo[0] - m, x1 = seed.x + hi[0] + m, y0 = seed.y + lo[1] - m,
+                        y1 = seed.y + hi[1] + m, z0 = seed.z + lo[2] - m, z1 = seed.z + hi[2] + m;
+            if (x0 >= 0.f && x1 <= 1000.f && y0 >= 0.f && y1 <= 1000.f && z0 >= 0.f && z1 <= 1000.f) {
+              const int a0 = grid_axis(x0, fdim), a1 = grid_axis(x1, fdim) + 1;
+              const int b0 = grid_axis(y0, fdim), b1 = grid_axis(y1, fdim) + 1;
+              const int c0 = grid_axis(z0, fdim), c1 = grid_axis(z1, fdim) + 1;
+              const size_t W = (size_t)fdim + 1;
+              const unsigned* sat = field_sat + PD(sat_off);
+              auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
+              const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
+                                       at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
+              interior = touched == 0u;
+            }
           }
         }
         take = interior;
