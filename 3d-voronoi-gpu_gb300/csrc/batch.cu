@@ -40,6 +40,7 @@ struct vgb_batch {
   int n_prob = 0, n = 0, n_tet = 0, n_vert = 0;
   std::vector<ProbDesc> probs;   // host copy of the descriptors
   std::vector<int> site_cap;     // largest K each problem may take (n_p - 1, at most MAX_SITE_K)
+  std::vector<double> mesh_vol;  // volume of each problem's mesh
   long long ncell = 0, ncell_cap = 0, knn_cap = 0;
   int kmax = 0;
   float density = 3.1f;          // sites per grid cell
@@ -112,12 +113,7 @@ void drop_graphs(vgb_batch* b) {
     }
 }
 
-// Grid side of a problem of n sites at `density` sites per cell (at 3.1,
-// vgb_grid_dim's value: the reference's round((n / 3.1)^(1/3))).
-int batch_dim(int n, float density) {
-  int d = (int)std::round(std::pow(n / density, 1.0f / 3.0));
-  return d < 1 ? 1 : d;
-}
+
 
 // Lay the problems out for the current K and density: cell and neighbour-row
 // offsets, descriptors on the device, tets sorted by centroid cell and their
@@ -126,7 +122,7 @@ int layout(vgb_batch* b) {
   long long cell = 0, knn = 0;
   int kmax = 1;
   for (auto& P : b->probs) {
-    P.dim = batch_dim(P.n_site, b->density);
+    P.dim = site_grid_dim(P.n_site, b->mesh_vol[&P - b->probs.data()], b->density);
     P.cell_off = (int)cell;
     cell += (long long)P.dim * P.dim * P.dim;
     P.knn_off = knn;
@@ -205,6 +201,7 @@ struct HostProblem {
   std::vector<unsigned> sat;
   float rt_max = 0.f;
   int fdim = 8;
+  double vol = 0.0;
 };
 
 void prepare_problem(const float* verts, int nv, const int* tets, int nt, int n_site, HostProblem& h) {
@@ -231,6 +228,7 @@ void prepare_problem(const float* verts, int nv, const int* tets, int nt, int n_
                      a[2] * (e[0] * f[1] - e[1] * f[0])) / 6.0;
   }
   h.rt_max = rt * 1.001f + 1e-3f;
+  h.vol = mesh_volume(verts, tets, nt);
   // field cells about a third of the site spacing, at most 256 per side
   const double spacing = std::cbrt(std::max(vol, 1.0) / std::max(n_site, 1));
   h.fdim = (int)std::min(256.0, std::max(8.0, std::ceil(3000.0 / spacing)));
@@ -301,6 +299,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
   // descriptors (K and grid set by layout / the autotuner)
   b->probs.resize(n_prob);
   b->site_cap.resize(n_prob);
+  b->mesh_vol.resize(n_prob);
   long long s_off = 0, t_off = 0, f_off = 0, q_off = 0, knn_cap = 0, cell_cap = 0;
   const float finest = 1.5f;  // densest grid the autotuner tries
   for (int p = 0; p < n_prob; ++p) {
@@ -321,7 +320,8 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     f_off += (long long)hp[p].inside.size();
     q_off += (long long)hp[p].sat.size();
     knn_cap += (long long)n_site[p] * std::min(cfg.site_k > 0 ? cfg.site_k : MAX_SITE_K, b->site_cap[p]);
-    const long long d = batch_dim(n_site[p], finest);
+    b->mesh_vol[p] = hp[p].vol;
+    const long long d = site_grid_dim(n_site[p], hp[p].vol, finest);
     cell_cap += d * d * d;
   }
   b->knn_cap = knn_cap;

@@ -325,7 +325,13 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   e->K = cfg.site_k > 0 ? cfg.site_k : k_cap;
   e->tk = vgb_tet_k(n_site, n_tet, cfg.tet_k);
   if (e->tk > MAX_TET_K) { set_error("tet_k=%d above %d", e->tk, MAX_TET_K); delete e; return VGB_ERR_INVALID; }
-  e->dim = cfg.grid_dim > 0 ? cfg.grid_dim : vgb_grid_dim(n_site);
+  // exact form: grid sized by the sites' density inside the mesh (a torus
+  // filling 15% of the box gets cells 1.9x finer than the reference's
+  // heuristic, which counts sites over the whole box)
+  const bool exact_grid = cfg.method == VGB_METHOD_CELL_TET && cfg.exact;
+  e->dim = cfg.grid_dim > 0 ? cfg.grid_dim
+           : exact_grid     ? site_grid_dim(n_site, mesh_volume(verts, tets, n_tet), 3.1f)
+                            : vgb_grid_dim(n_site);
   e->ncell = (long long)e->dim * e->dim * e->dim;
   if (e->ncell >= (1LL << 31) - 1) { set_error("grid too large"); delete e; return VGB_ERR_INVALID; }
   e->prob = lone_problem(n_site, e->dim, n_tet, e->K);

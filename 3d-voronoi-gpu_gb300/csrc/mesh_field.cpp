@@ -29,6 +29,31 @@ static inline int axis_cell(float p, int dim) {
   return i < 0 ? 0 : (i > dim - 1 ? dim - 1 : i);
 }
 
+double mesh_volume(const float* verts, const int* tets, int nt) {
+  double vol = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    const float* p[4];
+    for (int q = 0; q < 4; ++q) p[q] = verts + 3 * (size_t)tets[4 * (size_t)t + q];
+    double a[3], b[3], c[3];
+    for (int d = 0; d < 3; ++d) {
+      a[d] = (double)p[1][d] - p[0][d];
+      b[d] = (double)p[2][d] - p[0][d];
+      c[d] = (double)p[3][d] - p[0][d];
+    }
+    vol += std::fabs(a[0] * (b[1] * c[2] - b[2] * c[1]) + a[1] * (b[2] * c[0] - b[0] * c[2]) +
+                     a[2] * (b[0] * c[1] - b[1] * c[0])) / 6.0;
+  }
+  return vol;
+}
+
+int site_grid_dim(int n_site, double mesh_vol, float density) {
+  // sites per cell counted inside the mesh, not over the whole box: a mesh
+  // filling a fraction f of [0,1000]^3 gets f^(-1/3) times finer cells
+  const double fill = mesh_vol > 0.0 ? std::min(1.0, mesh_vol / 1e9) : 1.0;
+  const int d = (int)std::lround(std::cbrt((double)n_site / (density * fill)));
+  return d < 1 ? 1 : d;
+}
+
 int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim,
                        std::vector<unsigned char>& inside, std::vector<unsigned>& sat) {
   const long long nc = (long long)dim * dim * dim;

@@ -232,6 +232,12 @@ int clip_prepare();
 
 #include <vector>
 namespace vgb {
+// Volume of a tet mesh (host, double).
+double mesh_volume(const float* verts, const int* tets, int nt);
+// Site-grid side for n sites in a mesh of that volume at `density` sites per
+// cell of the mesh (the exact and batched forms; the reference form keeps
+// vgb_grid_dim, the reference's heuristic over the whole box).
+int site_grid_dim(int n_site, double mesh_vol, float density);
 // Inside field of a mesh on a dim^3 grid over [0,1000]^3 (mesh_field.cpp).
 int build_inside_field(const float* verts, int nv, const int* tets, int nt, int dim, std::vector<unsigned char>& inside,
                        std::vector<unsigned>& sat);

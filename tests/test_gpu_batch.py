@@ -25,7 +25,7 @@ def _lone(pkg, P, K, n_iter):
         mom = np.empty_like(mom_g)
         vol[ids] = vol_g
         mom[ids] = mom_g
-        return E.sites_original(), vol, mom
+        return E.sites_original(), vol, mom, E.grid_dim
 
 
 @pytest.mark.parametrize("use_graph", [True, False])
@@ -40,9 +40,9 @@ def test_batch_matches_lone_engines(pkg, meshgen, use_graph):
         B.sync()
         for p, P in enumerate(probs):
             info = B.problem(p)
-            assert info["site_k"] == K and info["grid_dim"] == pkg.lib().vgb_grid_dim(len(P.sites))
             xyz, vol, mom = B.result(p)
-            rx, rv, rm = _lone(pkg, P, K, 2)
+            rx, rv, rm, rdim = _lone(pkg, P, K, 2)
+            assert info["site_k"] == K and info["grid_dim"] == rdim
             assert np.array_equal(vol, rv), p
             assert np.array_equal(mom, rm), p
             assert np.array_equal(xyz, rx), p

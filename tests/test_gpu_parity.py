@@ -51,6 +51,16 @@ def check_moments(oracle, P, g, ref):
     return rel.max(), err
 
 
+def by_id(d):
+    """Volumes and moments of a pass in input (id) order."""
+    out = dict(d)
+    for k in ("vol", "mom"):
+        a = np.empty_like(d[k])
+        a[d["ids"]] = d[k]
+        out[k] = a
+    return out
+
+
 def oracle_pass(oracle, g, P, K):
     """Oracle on the GPU's sorted sites: sort order, kNN, candidates, moments."""
     return oracle.iteration(P.sites, P.verts, P.tets, K, g["tk"])
@@ -226,9 +236,10 @@ def test_exact_form_matches_oracle(built, meshgen, oracle):
         g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats(), tk=e.tet_k)
         g["vol"], g["mom"] = e.moments()
     r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
-    assert np.array_equal(g["ids"], r["ids"])
+    # the exact form sizes its grid by the sites' density in the mesh, so
+    # its grid order may differ from the oracle's: compare by site id
     assert g["stats"]["interior"] > len(P.sites) // 5
-    check_moments(oracle, P, g, r)
+    check_moments(oracle, P, by_id(g), by_id(r))
 
 
 def test_exact_form_on_torus(built, meshgen, oracle):
@@ -243,6 +254,5 @@ def test_exact_form_on_torus(built, meshgen, oracle):
         g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
         g["vol"], g["mom"] = e.moments()
     r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
-    assert np.array_equal(g["ids"], r["ids"])
     assert g["stats"]["interior"] > 0
-    check_moments(oracle, P, g, r)
+    check_moments(oracle, P, by_id(g), by_id(r))
