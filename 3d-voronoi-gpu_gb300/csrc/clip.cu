@@ -21,9 +21,10 @@
 //     Planes come nearest first, so a lane stops as soon as the plane
 //     distance exceeds twice its tet's farthest corner;
 //   * surviving tets are clipped by the whole warp: the cell's vertices (dual
-//     triangles, three plane ids each) are spread over the lanes, four slots
-//     per lane, with their coordinates cached in registers, so a conflict test
-//     is one 4-term dot product per vertex and a ballot;
+//     triangles, three plane ids each) are spread over the lanes, three
+//     slots per lane (96 vertices, the reference's triangle capacity), with
+//     their coordinates cached in registers, so a conflict test is one 4-term
+//     dot product per vertex and a ballot;
 //   * the cavity boundary is found in parallel: a directed edge of a removed
 //     triangle is on the boundary when no other removed triangle holds its
 //     twin -- one lane per edge and a __match_any_sync on the undirected edge
@@ -110,7 +111,11 @@ __device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int
       S.mtri[k * WARP + lane] = c.tri[k];
       S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
     }
-  if (lane < TRI_SLOTS) S.mvm[lane] = c.vm[lane == 0 ? 0 : lane == 1 ? 1 : lane == 2 ? 2 : 3];
+  unsigned my_vm = c.vm[0];
+#pragma unroll
+  for (int k = 1; k < TRI_SLOTS; ++k)
+    if (lane == k) my_vm = c.vm[k];
+  if (lane < TRI_SLOTS) S.mvm[lane] = my_vm;
   if (lane == 0) {
     S.mnt = c.nt;
     S.mr2 = c.r2;
@@ -130,7 +135,7 @@ __device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int
 //     method's per-tet cells;
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
 template <bool CELL_TET, bool BATCHED>
-__global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
     const int4* __restrict__ tets, const int* __restrict__ site_start, const int* __restrict__ site_tets,
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 6) k_clip_site(
       int state = 0;  // 0 kept, 1 empty, 2 dropped
       bool secmiss = bis;
       // counters of the sequence, packed: planes (bits 0-7), cuts (8-15),
-      // vertex-vs-plane tests (16-31); at most 138 planes of 128 vertices
+      // vertex-vs-plane tests (16-31); at most 144 planes of 96 vertices
       unsigned seq_cnt = 0u;
       const bool need_r2 = job != 2 || !CELL_TET;
       for (int pi = pbeg; pi < pend; ++pi) {

@@ -45,7 +45,7 @@ enum StatSlot : int {
 constexpr int WARP = 32;
 constexpr int MAX_SITE_K = 128;   // largest supported site-kNN K
 constexpr int MAX_TET_K = 128;    // largest supported candidates per tet
-constexpr int TRI_SLOTS = 4;      // triangles per lane in the clip kernel
+constexpr int TRI_SLOTS = 3;      // triangles per lane in the clip kernel (96 per cell, as the reference)
 constexpr int MAX_TRI = WARP * TRI_SLOTS;
 
 // Grid of the reference (knearests.cu:19-27, :243): dim^3 cells over
