@@ -188,18 +188,23 @@ def measured_peaks():
     return 6800.0, 2070.0, "fallback"
 
 
-def profile_traffic(kernel: str, workload: str):
-    """Per-launch DRAM bytes from a committed ncu summary, if one exists."""
+def profile_value(kernel: str, workload: str, key: str = "traffic_bytes_per_launch"):
+    """A per-launch figure (`key: value` line) from a committed ncu summary, if one exists."""
     p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profile_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes from a committed ncu summary, if one exists."""
+    return profile_value(kernel, workload)
 
 
 # ---------------------------------------------------------------------------
@@ -399,6 +404,17 @@ def run_ours(args):
                     "traffic": profile_traffic("knn_sites", args.workload),
                     "peak_source": f"{peak_src} hbm_gbs", "bytes_per_launch": knn_bytes,
                     "ms_per_launch": round(phases["knn"], 4)}
+    # the clip's real bound: warp instructions issued per second (count from
+    # the committed ncu capture of the same workload) against 152 SMs x 4
+    # schedulers x the max SM clock
+    issue_peak = 152 * 4 * sm_max * 1e6 / 1e9   # G warp-instructions/s
+    roofline_issue = None
+    winst = profile_value("clip_exact" if exact else "clip_cell_tet", args.workload, "warp_instructions_per_launch")
+    if winst:
+        ach = winst / (phases["clip"] / 1e3) / 1e9
+        roofline_issue = {"kernel": kname, "bound": "issue", "achieved": round(ach, 1), "peak": round(issue_peak, 1),
+                          "unit": "G warp-inst/s", "frac": round(ach / issue_peak, 4),
+                          "warp_instructions_per_launch": winst, "ms_per_launch": round(phases["clip"], 4)}
 
     accuracy = None
     if args.accuracy > 0 and rank == 0:
@@ -444,6 +460,7 @@ def run_ours(args):
         "e2e": e2e,
         "roofline": roofline,
         "roofline_knn": roofline_knn,
+        "roofline_issue": roofline_issue,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "pairs_per_s": round(pairs_per_s, 1),
         "clipped_pairs_per_s": round(stats["clipped"] * value / world, 1),
