@@ -30,7 +30,7 @@ STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
 STAT_NAMES = ["candidates", "culled", "clipped", "empty", "contrib", "security_miss", "tri_overflow",
               "boundary_fail", "planes", "clips", "final_vertices", "conflict_tests", "cull_tests",
-              "new_vertices", "interior"]
+              "new_vertices", "interior", "redo"]
 PHASE_NAMES = ["grid", "knn", "candidates", "site_lists", "clip", "update"]
 BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6}
 METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}

@@ -55,21 +55,22 @@ constexpr int BOX_PLANES = 6;
 
 enum WarpCount : int {
   WC_CAND = 0, WC_CULLED, WC_CLIPPED, WC_EMPTY, WC_CONTRIB, WC_SECMISS, WC_OVERFLOW, WC_BOUNDARY, WC_PLANES,
-  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_N
+  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_REDO, WC_N
 };
 
+template <int SL>
 struct SiteSmem {
   float4 plane[4 + MAX_SITE_K + 2 * BOX_PLANES];  // 0..3 tet faces, 4+j bisector j, 4+K+b start-cube
                                                   // face b, 4+K+6+b domain-box face b
-  unsigned conf[MAX_TRI];                     // clip scratch: removed triangles
-  unsigned bedge[MAX_TRI];                    // clip scratch: boundary edges
+  unsigned conf[(WARP * SL)];                     // clip scratch: removed triangles
+  unsigned bedge[(WARP * SL)];                    // clip scratch: boundary edges
   unsigned queue[WARP];                       // surviving candidate tets of a chunk
   float4 corner[4];                           // corners of the tet being clipped
   unsigned cnt[WC_N];                         // per-warp counters (lane 0 writes)
   unsigned char faces[4 + MAX_SITE_K + BOX_PLANES];  // cell-tet: plane ids bounding the site's cell
-  unsigned mtri[MAX_TRI];                     // cell-tet: the site's cell
-  float4 mv[MAX_TRI];
-  unsigned mvm[TRI_SLOTS];
+  unsigned mtri[(WARP * SL)];                     // cell-tet: the site's cell
+  float4 mv[(WARP * SL)];
+  unsigned mvm[SL];
   int mnt;
   float mr2;
 };
@@ -83,11 +84,12 @@ __device__ __forceinline__ unsigned ord_key(float f) {
 __device__ __forceinline__ float ord_val(unsigned k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
-__device__ __forceinline__ void cell_bounds(const WarpCell& c, int lane, float lo[3], float hi[3]) {
+template <int SL>
+__device__ __forceinline__ void cell_bounds(const WarpCell<SL>& c, int lane, float lo[3], float hi[3]) {
   const unsigned lane_bit = 1u << lane;
   float l0 = FLT_MAX, l1 = FLT_MAX, l2 = FLT_MAX, h0 = -FLT_MAX, h1 = -FLT_MAX, h2 = -FLT_MAX;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k)
+  for (int k = 0; k < SL; ++k)
     if (c.vm[k] & lane_bit) {
       l0 = fminf(l0, c.vx[k]); h0 = fmaxf(h0, c.vx[k]);
       l1 = fminf(l1, c.vy[k]); h1 = fmaxf(h1, c.vy[k]);
@@ -103,19 +105,20 @@ __device__ __forceinline__ void cell_bounds(const WarpCell& c, int lane, float l
 
 // The site's cell into its shared copy, which the box bound and every tet
 // clip start from.
-__device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int lane) {
+template <int SL>
+__device__ __forceinline__ void store_master(const WarpCell<SL>& c, SiteSmem<SL>& S, int lane) {
   const unsigned lane_bit = 1u << lane;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k)
+  for (int k = 0; k < SL; ++k)
     if (c.vm[k] & lane_bit) {
       S.mtri[k * WARP + lane] = c.tri[k];
       S.mv[k * WARP + lane] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
     }
   unsigned my_vm = c.vm[0];
 #pragma unroll
-  for (int k = 1; k < TRI_SLOTS; ++k)
+  for (int k = 1; k < SL; ++k)
     if (lane == k) my_vm = c.vm[k];
-  if (lane < TRI_SLOTS) S.mvm[lane] = my_vm;
+  if (lane < SL) S.mvm[lane] = my_vm;
   if (lane == 0) {
     S.mnt = c.nt;
     S.mr2 = c.r2;
@@ -134,7 +137,7 @@ __device__ __forceinline__ void store_master(const WarpCell& c, SiteSmem& S, int
 //     reached (voronoi.cu:679-697): the cell-tet build and the tet-cell
 //     method's per-tet cells;
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
-template <bool CELL_TET, bool BATCHED>
+template <bool CELL_TET, bool BATCHED, int SL, bool REDO>
 __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
@@ -142,18 +145,25 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     dmom4* __restrict__ mom, unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, const int* __restrict__ tet_order,
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
-    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss) {
-  __shared__ SiteSmem smem_all[CLIP_WARPS];
+    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss, int* __restrict__ redo_list,
+    int* __restrict__ redo_count) {
+  __shared__ SiteSmem<SL> smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  SiteSmem& S = smem_all[wib];
+  SiteSmem<SL>& S = smem_all[wib];
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   if (lane < WC_N) S.cnt[lane] = 0u;
   unsigned cull_lane = 0;  // per-lane tet-vs-plane tests of the culling pass
   const bool exact = CELL_TET && tet_order != nullptr;
   __syncwarp();
 
-  for (int s = blockIdx.x * CLIP_WARPS + wib; s < n; s += gridDim.x * CLIP_WARPS) {
+  // REDO: the sites a capacity-2 pass gave up on (their cell outgrew it);
+  // otherwise every site, and a site that outgrows the capacity is handed on
+  // through redo_list when there is one
+  const int n_items = REDO ? *redo_count : n;
+  for (int it = blockIdx.x * CLIP_WARPS + wib; it < n_items; it += gridDim.x * CLIP_WARPS) {
+    const int s = REDO ? redo_list[it] : it;
+    bool abandon = false;
     // the site's problem; its descriptor fields are read where used (from
     // global memory or the kernel parameters) rather than held in registers
     const int pidx = BATCHED ? site_prob[s] : 0;
@@ -213,7 +223,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       // ---------------------------------------------------------------
       // the next cell: the site's cell, the same cell (from its shared copy)
       // for the box bound, or the next surviving candidate
-      WarpCell c;
+      WarpCell<SL> c;
       cell_clear(c);
       if (job == 0) {
         const float L = cube_half();
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         c.r2 = 3.f * L * L;
       } else if (job == 1) {
 #pragma unroll
-        for (int k = 0; k < TRI_SLOTS; ++k) {
+        for (int k = 0; k < SL; ++k) {
           c.vm[k] = S.mvm[k];
           if (c.vm[k] & lane_bit) {
             c.tri[k] = S.mtri[k * WARP + lane];
@@ -362,7 +372,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         }
         if (CELL_TET) {
 #pragma unroll
-          for (int k = 0; k < TRI_SLOTS; ++k) {
+          for (int k = 0; k < SL; ++k) {
             c.vm[k] = S.mvm[k];
             if (c.vm[k] & lane_bit) {
               c.tri[k] = S.mtri[k * WARP + lane];
@@ -405,6 +415,10 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         seq_cnt += 1u + ((unsigned)c.nt << 16);
         const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane, need_r2);
         if (r == CLIP_EMPTY) { state = 1; break; }
+        if (!REDO && r == CLIP_OVERFLOW && redo_list) {
+          abandon = true;
+          break;
+        }
         if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
           if (lane == 0) S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
           state = 2;
@@ -419,6 +433,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
         S.cnt[WC_CONFLICT] += seq_cnt >> 16;
       }
+      if (abandon) break;
       if (job == 2 && bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
 
       // ---------------------------------------------------------------
@@ -441,7 +456,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         if (state != 0) {
           // the box bound failed (degenerate): keep the unbounded cell
 #pragma unroll
-          for (int k = 0; k < TRI_SLOTS; ++k) {
+          for (int k = 0; k < SL; ++k) {
             c.vm[k] = S.mvm[k];
             if (c.vm[k] & lane_bit) {
               c.tri[k] = S.mtri[k * WARP + lane];
@@ -509,7 +524,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           // the planes that bound the cell (ids present in its triangles)
           unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
 #pragma unroll
-          for (int k = 0; k < TRI_SLOTS; ++k)
+          for (int k = 0; k < SL; ++k)
             if (c.vm[k] & lane_bit)
 #pragma unroll
               for (int e = 0; e < 3; ++e) {
@@ -562,6 +577,15 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       __syncwarp();
       if (interior) break;
     }
+    if (abandon) {
+      // the larger-capacity pass redoes this site from scratch
+      if (lane == 0) {
+        redo_list[atomicAdd(redo_count, 1)] = s;
+        S.cnt[WC_REDO]++;
+      }
+      __syncwarp();
+      continue;
+    }
     if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
     __syncwarp();
 #undef PD
@@ -573,23 +597,39 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     static const int slot[WC_N] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB,
                                    STAT_SECURITY_MISS, STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES,
                                    STAT_CLIPS, STAT_FINAL_VERTICES, STAT_CONFLICT_TESTS, STAT_CULL_TESTS,
-                                   STAT_NEW_VERTICES, STAT_INTERIOR};
+                                   STAT_NEW_VERTICES, STAT_INTERIOR, STAT_REDO};
     if (S.cnt[lane]) atomicAdd(stats + slot[lane], (unsigned long long)S.cnt[lane]);
   }
 }
 
-static int g_clip_resident_blocks[3] = {0, 0, 0};  // SMs x resident blocks per SM, per variant
+// Cell capacity (triangle slots per lane): the cell-tet form runs with 2
+// (64 vertices) and redoes the rare sites whose cell outgrows it with 4 (128);
+// the tet-cell method runs with 3 (96, the reference's capacity).
+constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
+
+// SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
+// fast / redo, cell-tet batched fast / redo
+static int g_clip_resident_blocks[5] = {0, 0, 0, 0, 0};
+
+template <class F>
+static int resident_blocks(F kernel, int sms, int* out) {
+  int per_sm = 0;
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, CLIP_WARPS * WARP, 0));
+  *out = sms * (per_sm > 0 ? per_sm : 1);
+  return 0;
+}
 
 int clip_prepare() {
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0;
   VGB_CUDA_TRY(cudaGetDevice(&dev));
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<false, false>, CLIP_WARPS * WARP, 0));
-  g_clip_resident_blocks[0] = sms * (per_sm > 0 ? per_sm : 1);
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<true, false>, CLIP_WARPS * WARP, 0));
-  g_clip_resident_blocks[1] = sms * (per_sm > 0 ? per_sm : 1);
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_clip_site<true, true>, CLIP_WARPS * WARP, 0));
-  g_clip_resident_blocks[2] = sms * (per_sm > 0 ? per_sm : 1);
+  int* r = g_clip_resident_blocks;
+  if (resident_blocks(k_clip_site<false, false, SLOTS_TET_CELL, false>, sms, r + 0) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_FAST, false>, sms, r + 1) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_REDO, true>, sms, r + 2) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_FAST, false>, sms, r + 3) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_REDO, true>, sms, r + 4))
+    return -2;
   return 0;
 }
 
@@ -598,33 +638,47 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, unsigned* prob_secmiss, cudaStream_t st) {
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* redo_list, int* redo_count,
+                    cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
   if (!cell_tet && probs) {
     set_error("the tet-cell method runs one problem at a time");
     return -1;
   }
+  if (cell_tet && !redo_list) {
+    set_error("the cell-tet clip needs its redo list");
+    return -1;
+  }
   // a few waves of resident blocks; sites are dealt round-robin to warps
-  const int variant = !cell_tet ? 0 : probs ? 2 : 1;
-  long long want = (long long)g_clip_resident_blocks[variant] * 4;
-  long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
-  int blocks = (int)(want < need ? want : need);
-  if (variant == 2)
-    k_clip_site<true, true><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts, tets,
-                                                                  site_start, site_tets, mom, stats, field,
-                                                                  field_sat, tet_order, tet_cell_start, tet_sph,
-                                                                  reach, reach_max_bits, prob_secmiss);
-  else if (variant == 1)
-    k_clip_site<true, false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts,
-                                                                   tets, site_start, site_tets, mom, stats, field,
-                                                                   field_sat, tet_order, tet_cell_start, tet_sph,
-                                                                   reach, reach_max_bits, prob_secmiss);
-  else
-    k_clip_site<false, false><<<blocks, CLIP_WARPS * WARP, 0, st>>>(sites, n, knn, probs, site_prob, lone, verts,
-                                                                    tets, site_start, site_tets, mom, stats, nullptr,
-                                                                    nullptr, nullptr, nullptr, nullptr, nullptr,
-                                                                    nullptr, prob_secmiss);
+  auto blocks_for = [&](int variant) {
+    const long long want = (long long)g_clip_resident_blocks[variant] * 4;
+    const long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
+    return (int)(want < need ? want : need);
+  };
+  if (!cell_tet) {
+    k_clip_site<false, false, SLOTS_TET_CELL, false><<<blocks_for(0), CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
+        nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr);
+    VGB_CUDA_TRY(cudaGetLastError());
+    return 0;
+  }
+  VGB_CUDA_TRY(cudaMemsetAsync(redo_count, 0, sizeof(int), st));
+  if (probs) {
+    k_clip_site<true, true, SLOTS_FAST, false><<<blocks_for(3), CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
+        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+    k_clip_site<true, true, SLOTS_REDO, true><<<g_clip_resident_blocks[4], CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
+        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+  } else {
+    k_clip_site<true, false, SLOTS_FAST, false><<<blocks_for(1), CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
+        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+    k_clip_site<true, false, SLOTS_REDO, true><<<g_clip_resident_blocks[2], CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
+        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+  }
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -3,7 +3,8 @@
 // A convex cell is kept as its dual triangulation, as in the reference
 // (voronoi.h:20-76): planes n.x + w >= 0 (inside), and triangles = three
 // plane ids = one vertex of the cell.  Here the triangles are spread over the
-// 32 lanes of a warp, TRI_SLOTS slots per lane; slot (k, lane) is live when
+// 32 lanes of a warp, SL slots per lane (a template parameter: the capacity is
+// 32 SL triangles); slot (k, lane) is live when
 // bit `lane` of vm[k] is set (vm is the same in every lane).  Each live slot
 // caches its vertex (x, y, z) and |x|^2 in registers, so testing a plane is
 // one 3-FMA evaluation per vertex and a ballot.  Plane equations live in
@@ -19,10 +20,11 @@ constexpr unsigned FULL = 0xffffffffu;
 
 enum ClipResult : int { CLIP_NONE = 0, CLIP_CUT = 1, CLIP_EMPTY = 2, CLIP_OVERFLOW = 3, CLIP_BOUNDARY = 4 };
 
+template <int SL>
 struct WarpCell {
-  unsigned tri[TRI_SLOTS];
-  float vx[TRI_SLOTS], vy[TRI_SLOTS], vz[TRI_SLOTS], vw[TRI_SLOTS];
-  unsigned vm[TRI_SLOTS];
+  unsigned tri[SL];
+  float vx[SL], vy[SL], vz[SL], vw[SL];
+  unsigned vm[SL];
   int nt;    // live triangles (warp-uniform)
   float r2;  // max |vertex|^2 over live triangles (warp-uniform)
 };
@@ -87,9 +89,10 @@ struct CompSum {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-__device__ __forceinline__ void cell_clear(WarpCell& c) {
+template <int SL>
+__device__ __forceinline__ void cell_clear(WarpCell<SL>& c) {
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k) {
+  for (int k = 0; k < SL; ++k) {
     c.tri[k] = 0u;
     c.vx[k] = c.vy[k] = c.vz[k] = c.vw[k] = 0.f;
     c.vm[k] = 0u;
@@ -108,16 +111,17 @@ __device__ __forceinline__ void cell_clear(WarpCell& c) {
 // ten triangles).  Each boundary vertex must start and end exactly one
 // boundary edge, else the cell is dropped (the reference's
 // inconsistent_boundary).  New triangles fill freed slots; the receiving lane
-// computes the new vertex.  conf and bedge are MAX_TRI-entry scratch arrays of
+// computes the new vertex.  conf and bedge are 32 SL-entry scratch arrays of
 // the warp.  need_r2: keep c.r2 (the largest |vertex|^2) current; callers that
 // never read it skip the warp reduction.
-__device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsigned pidx, const float4* planes,
+template <int SL>
+__device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
                                          unsigned* conf, unsigned* bedge, const int lane, const bool need_r2) {
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
-  unsigned m[TRI_SLOTS];
+  unsigned m[SL];
   int nconf = 0;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k) {
+  for (int k = 0; k < SL; ++k) {
     m[k] = 0u;
     if (c.vm[k]) {
       bool cf = (c.vm[k] & lane_bit) && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
@@ -130,7 +134,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
   {
     int off = 0;
 #pragma unroll
-    for (int k = 0; k < TRI_SLOTS; ++k) {
+    for (int k = 0; k < SL; ++k) {
       if (!m[k]) continue;
       if (m[k] & lane_bit) conf[off + __popc(m[k] & lt_mask)] = c.tri[k];
       off += __popc(m[k]);
@@ -183,7 +187,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
       unsigned bm = __ballot_sync(FULL, isb);
       if (isb) {
         int r = nb + __popc(bm & lt_mask);
-        if (r < MAX_TRI) bedge[r] = ea | (eb << 8);
+        if (r < (WARP * SL)) bedge[r] = ea | (eb << 8);
       }
       nb += __popc(bm);
     }
@@ -196,7 +200,7 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
       const unsigned ga = __match_any_sync(FULL, ka);
       const unsigned gb = __match_any_sync(FULL, kb);
       bad = live && (__popc(ga) != 1 || __popc(gb) != 1);
-    } else if (nb <= MAX_TRI) {
+    } else if (nb <= (WARP * SL)) {
       for (int e = lane; e < nb; e += WARP) {
         unsigned E = bedge[e];
         int starts = 0, ends = 0;
@@ -211,14 +215,14 @@ __device__ __forceinline__ int warp_clip(WarpCell& c, const float4 P, const unsi
     bad = __any_sync(FULL, bad);
   }
   const int nt2 = c.nt - R + nb;
-  if (nt2 > MAX_TRI) return CLIP_OVERFLOW;
+  if (nt2 > (WARP * SL)) return CLIP_OVERFLOW;
   if (bad || nb < 3) return CLIP_BOUNDARY;
   __syncwarp();
   float lm = 0.f;
   int base = 0;
   bool nonfinite = false;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k) {
+  for (int k = 0; k < SL; ++k) {
     if (c.vm[k] == 0u && base >= nb) continue;  // empty slot, nothing left to place
     const unsigned keep = c.vm[k] & ~m[k];
     const unsigned freem = ~keep;
@@ -289,18 +293,19 @@ __device__ __forceinline__ void vertex_moments(float3 A, float4 p0, float4 p1, f
 // the warp.  The decomposition is taken from the mean of the cell's vertices
 // (any apex gives the same sums; an inside apex avoids cancellation), and
 // the reference's |vol| < 0.1 cut (voronoi.cu:599) is not applied.
-__device__ __forceinline__ void warp_moments(const WarpCell& c, const float4* planes, const int lane, float& vol,
+template <int SL>
+__device__ __forceinline__ void warp_moments(const WarpCell<SL>& c, const float4* planes, const int lane, float& vol,
                                              float& mx, float& my, float& mz) {
   const unsigned lane_bit = 1u << lane;
   float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k)
+  for (int k = 0; k < SL; ++k)
     if (c.vm[k] & lane_bit) { sx += c.vx[k]; sy += c.vy[k]; sz += c.vz[k]; }
   const float inv = __frcp_rn((float)c.nt);
   const float cx = warp_sum(sx) * inv, cy = warp_sum(sy) * inv, cz = warp_sum(sz) * inv;
   float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
 #pragma unroll
-  for (int k = 0; k < TRI_SLOTS; ++k) {
+  for (int k = 0; k < SL; ++k) {
     if (c.vm[k] & lane_bit) {
       const unsigned T = c.tri[k];
       float4 q0 = planes[tri_at(T, 0)], q1 = planes[tri_at(T, 1)], q2 = planes[tri_at(T, 2)];

@@ -58,6 +58,8 @@ struct vgb_engine {
   float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
   float4* tet_sph = nullptr;       // exact form: tet bounding spheres (centroid-cell order)
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
+  int* redo_list = nullptr;        // cell-tet: sites handed from the 64- to the 128-vertex pass (n)
+  int* redo_count = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -170,7 +172,8 @@ void free_engine(vgb_engine* e) {
     if (ev) cudaEventDestroy(ev);
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
-                  e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph};
+                  e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph,
+                  e->redo_list, e->redo_count};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -211,7 +214,7 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
-                        e->reach_max, nullptr, st))
+                        e->reach_max, nullptr, e->redo_list, e->redo_count, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -352,7 +355,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, n_site)) || (rc = dalloc(&e->redo_count, 1)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
     free_engine(e);

@@ -39,14 +39,13 @@ enum StatSlot : int {
   STAT_CULL_TESTS = 12,      // tet-vs-plane tests of the separation pass
   STAT_NEW_VERTICES = 13,    // vertices created by clipping
   STAT_INTERIOR = 14,        // sites whose whole cell lies inside the mesh (taken whole)
+  STAT_REDO = 15,            // sites redone with the larger cell capacity (their cell outgrew 64 vertices)
   STAT_COUNT = 16
 };
 
 constexpr int WARP = 32;
 constexpr int MAX_SITE_K = 128;   // largest supported site-kNN K
 constexpr int MAX_TET_K = 128;    // largest supported candidates per tet
-constexpr int TRI_SLOTS = 3;      // triangles per lane in the clip kernel (96 per cell, as the reference)
-constexpr int MAX_TRI = WARP * TRI_SLOTS;
 
 // Grid of the reference (knearests.cu:19-27, :243): dim^3 cells over
 // [0,1000]^3, a point's cell is floor(p * dim / 1000) clamped, in float.
@@ -206,9 +205,11 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, unsigned* prob_secmiss, cudaStream_t st);
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* redo_list, int* redo_count,
+                    cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
-// reached the security radius.
+// reached the security radius.  redo_list (n ints) and redo_count (1 int):
+// cell-tet scratch for the sites a 64-vertex pass hands to a 128-vertex one.
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.

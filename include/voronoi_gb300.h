@@ -60,6 +60,7 @@ enum vgb_stat {
   VGB_STAT_CULL_TESTS = 12,     /* tet-vs-plane tests of the separation pass          */
   VGB_STAT_NEW_VERTICES = 13,   /* vertices created by clipping                       */
   VGB_STAT_INTERIOR = 14,       /* sites whose whole cell lies inside the mesh        */
+  VGB_STAT_REDO = 15,           /* sites redone at 128 vertices (outgrew 64)          */
   VGB_STAT_COUNT = 16
 };
 

@@ -256,3 +256,37 @@ def test_exact_form_on_torus(built, meshgen, oracle):
     r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
     assert g["stats"]["interior"] > 0
     check_moments(oracle, P, by_id(g), by_id(r))
+
+
+def test_large_cells_redone(built, meshgen, oracle):
+    """A site ringed by 44 close neighbours has a cell of about 84 vertices:
+    the 64-vertex pass of the cell-tet clip hands it (and any other site that
+    outgrows 64) to the 128-vertex pass, and the moments still match the
+    oracle."""
+    pkg = built
+    base = meshgen.cube_problem(6, 1500, seed=3)
+    c = np.array([500.0, 500.0, 500.0])
+    far = np.linalg.norm(base.sites - c, axis=1) > 100.0
+    m = 44
+    i = np.arange(m) + 0.5
+    phi, th = np.arccos(1.0 - 2.0 * i / m), np.pi * (1.0 + 5.0 ** 0.5) * i
+    # radii jittered: cospherical neighbours would make their bisectors meet
+    # in one point (degenerate vertices, which float predicates cannot order)
+    rad = 20.0 * (1.0 + 0.05 * np.random.default_rng(5).uniform(-1.0, 1.0, m))
+    ring = c + rad[:, None] * np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], axis=1)
+    sites = np.concatenate([base.sites[far], c[None], ring]).astype(np.float32)
+    P = meshgen.Problem("ring", base.verts, base.tets, sites)
+    tk = 128
+    # K = 128: the ring's elongated cells reach their security radius, so
+    # both sides compute complete cells (at 64 they do not, and the two forms
+    # then clip an incomplete cell against different tet sets)
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=128, tet_k=tk, exact=True) as e:
+        e.iterate(1, update=False)
+        e.sync()
+        s4 = e.buffer("sites")
+        g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
+        g["vol"], g["mom"] = e.moments()
+    assert g["stats"]["redo"] >= 1
+    assert g["stats"]["tri_overflow"] == 0 and g["stats"]["boundary_fail"] == 0
+    r = oracle.iteration(P.sites, P.verts, P.tets, 128, tk)
+    check_moments(oracle, P, by_id(g), by_id(r))
