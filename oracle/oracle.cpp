@@ -25,7 +25,10 @@
 //     that, compiled with -ffp-contract=off, it reproduces a host build of the
 //     reference bit for bit.  Used to pin this restatement.
 //   FIXED (double): the same steps in double with both thresholds removed and
-//     large capacities.  This is the accuracy oracle the GPU path is held to.
+//     large capacities, and the edge feet of the moment decomposition taken
+//     from the edge direction (a site lying exactly on a tet face plane, which
+//     float32 lattice meshes make happen, loses volume in the shipped form).
+//     This is the accuracy oracle the GPU path is held to.
 //
 // Distances for neighbour selection use d = fma(dz,dz, fma(dy,dy, dx*dx)) in
 // float, the contraction nvcc applies to the reference's distance expressions
@@ -351,9 +354,22 @@ struct Cell {
       V4<R> P[6];
       for (int i = 0; i < 3; ++i) P[2 * i] = project(C, pl[tr[t][i]]);
       for (int i = 0; i < 3; ++i) {
-        V4<R> n = cross3(sub4(P[2 * i], C), sub4(P[(2 * (i + 1)) % 6], C));
-        V4<R> pn = mk<R>(n.x, n.y, n.z, -dot3(C, n));
-        P[2 * i + 1] = project(A2, pn);
+        if (SHIPPED) {
+          V4<R> n = cross3(sub4(P[2 * i], C), sub4(P[(2 * (i + 1)) % 6], C));
+          V4<R> pn = mk<R>(n.x, n.y, n.z, -dot3(C, n));
+          P[2 * i + 1] = project(A2, pn);
+        } else {
+          // Foot of the seed on the edge line through A2, the line's direction
+          // being the cross product of the two face normals.  Equal to the
+          // projection above whenever the seed lies off both faces; when it
+          // lies on one (a site on a mesh lattice plane), the plane through
+          // C and the two face feet is undefined there and the projection
+          // collapses onto A2, dropping the pieces on either side.
+          V4<R> u = cross3(pl[tr[t][i]], pl[tr[t][(i + 1) % 3]]);
+          R u2 = dot3(u, u);
+          R lambda = u2 != R(0) ? dot3(sub4(C, A2), u) / u2 : R(0);
+          P[2 * i + 1] = add4(A2, scale3(lambda, u));
+        }
       }
       for (int i = 0; i < 6; ++i) {
         V4<R> a = P[i], b = P[(i + 1) % 6];

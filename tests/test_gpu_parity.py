@@ -290,3 +290,36 @@ def test_large_cells_redone(built, meshgen, oracle):
     assert g["stats"]["tri_overflow"] == 0 and g["stats"]["boundary_fail"] == 0
     r = oracle.iteration(P.sites, P.verts, P.tets, 128, tk)
     check_moments(oracle, P, by_id(g), by_id(r))
+
+
+@pytest.mark.parametrize("form", ["cell_tet", "site_major", "exact"])
+def test_sites_on_tet_face_planes(built, meshgen, oracle, form):
+    """Half the sites moved onto lattice planes of the Kuhn mesh (float32
+    equal to the vertices' z): each lies on a face plane of the tets around
+    it, the case where the shipped moment decomposition drops pieces.  The
+    GPU's fan from the cell's vertex centroid has no such case; the oracle
+    is its corrected double form."""
+    pkg = built
+    P0 = meshgen.cube_problem(20, 20000, seed=1)
+    s = P0.sites.copy()
+    planes = np.unique(P0.verts[:, 2])
+    on = np.arange(0, len(s), 2)
+    s[on, 2] = planes[np.abs(planes[None, :] - s[on, 2][:, None]).argmin(1)]
+    P = meshgen.Problem("cube20_on_planes", P0.verts, P0.tets, s)
+    mv = oracle.mesh_volume(P.verts, P.tets)
+    if form == "exact":
+        tk = 100
+        with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, tet_k=tk, exact=True) as e:
+            e.iterate(1, update=False)
+            e.sync()
+            s4 = e.buffer("sites")
+            g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
+            g["vol"], g["mom"] = e.moments()
+        r = oracle.iteration(P.sites, P.verts, P.tets, 64, tk)
+        check_moments(oracle, P, by_id(g), by_id(r))
+    else:
+        g = run_pass(pkg, P, 64, method=form)
+        r = oracle_pass(oracle, g, P, 64)
+        check_moments(oracle, P, g, r)
+    # every site keeps its volume: none loses the pieces beside its plane
+    assert abs(r["vol"].sum() / mv - 1) < 1e-4

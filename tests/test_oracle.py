@@ -123,6 +123,36 @@ def test_fixed_oracle_conserves_volume(meshgen, oracle):
     assert np.allclose(c["mom"], f["mom"], rtol=1e-9, atol=1e-3)
 
 
+def test_fixed_oracle_sites_on_tet_face_planes(meshgen, oracle):
+    # A float32 site can sit exactly on a lattice plane of a Kuhn mesh, so on a
+    # face plane of the tets around it.  The shipped moment decomposition
+    # (voronoi.cu:577-597) then drops the pieces beside that face; FIXED must
+    # still conserve the mesh volume and agree between both methods.
+    P = meshgen.cube_problem(6, 800, seed=11)
+    s = P.sites.copy()
+    planes = np.unique(P.verts[:, 2])
+    on = np.arange(0, len(s), 2)
+    s[on, 2] = planes[np.abs(planes[None, :] - s[on, 2][:, None]).argmin(1)]
+    assert np.isin(s[on, 2], P.verts[:, 2]).all()
+    nbr, _ = oracle.knn(s, None, 128)
+    cand, _ = oracle.knn(s, oracle.tet_centroids(P.verts, P.tets), 200, exclude_self=False)
+    mv = oracle.mesh_volume(P.verts, P.tets)
+    f = oracle.tet_cell(s, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
+    assert f["hist"][7 + 3] == 0
+    assert abs(f["vol"].sum() / mv - 1) < 1e-12
+    c = oracle.cell_tet(s, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
+    assert abs(c["vol"].sum() / mv - 1) < 1e-12
+    assert np.allclose(c["vol"], f["vol"], rtol=1e-9, atol=1e-6)
+    assert np.allclose(c["mom"], f["mom"], rtol=1e-9, atol=1e-3)
+    # the moments are those of the unsnapped decomposition's geometry: the
+    # sum of first moments is the mesh's own
+    corners = P.verts[P.tets].astype(np.float64)
+    tv = np.abs(np.einsum("ij,ij->i", corners[:, 0] - corners[:, 3],
+                          np.cross(corners[:, 1] - corners[:, 3], corners[:, 2] - corners[:, 3]))) / 6
+    mesh_mom = (tv[:, None] * corners.mean(1)).sum(0)
+    assert np.allclose(f["mom"].sum(0), mesh_mom, rtol=1e-10)
+
+
 def test_fixed_oracle_lattice_sites_have_equal_cells(meshgen, oracle):
     # sites near the centres of a 5^3 lattice of the mesh box: (nearly) equal
     # cubic cells.  The exact lattice is degenerate (eight cells share each
