@@ -157,11 +157,24 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   const bool exact = CELL_TET && tet_order != nullptr;
   __syncwarp();
 
-  // REDO: the sites a capacity-2 pass gave up on (their cell outgrew it);
-  // otherwise every site, and a site that outgrows the capacity is handed on
-  // through redo_list when there is one
+  // REDO: the sites a smaller-capacity pass gave up on (their cell outgrew
+  // it); otherwise every site, and a site that outgrows the capacity is
+  // handed on through redo_list when there is one.  With redo_count given,
+  // warps take the next item from a counter (redo_count[1] for the first
+  // pass, [2] for the redo pass) in a single wave of resident blocks, so a
+  // warp that drew cheap sites takes more; the tet-cell method deals items
+  // round-robin.
   const int n_items = REDO ? *redo_count : n;
-  for (int it = blockIdx.x * CLIP_WARPS + wib; it < n_items; it += gridDim.x * CLIP_WARPS) {
+  int* const work = redo_count ? redo_count + (REDO ? 2 : 1) : nullptr;
+  auto next_item = [&](int cur) {
+    if (work) {
+      int v = 0;
+      if (lane == 0) v = atomicAdd(work, 1);
+      return __shfl_sync(FULL, v, 0);
+    }
+    return cur + (int)gridDim.x * CLIP_WARPS;
+  };
+  for (int it = work ? next_item(0) : blockIdx.x * CLIP_WARPS + wib; it < n_items; it = next_item(it)) {
     const int s = REDO ? redo_list[it] : it;
     bool abandon = false;
     // the site's problem; its descriptor fields are read where used (from
@@ -650,9 +663,10 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     set_error("the cell-tet clip needs its redo list");
     return -1;
   }
-  // a few waves of resident blocks; sites are dealt round-robin to warps
+  // the cell-tet passes: one wave of resident blocks whose warps draw sites
+  // from a counter; the tet-cell method: a few waves, sites dealt round-robin
   auto blocks_for = [&](int variant) {
-    const long long want = (long long)g_clip_resident_blocks[variant] * 4;
+    const long long want = (long long)g_clip_resident_blocks[variant] * (variant == 0 ? 4 : 1);
     const long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
     return (int)(want < need ? want : need);
   };
@@ -663,7 +677,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
-  VGB_CUDA_TRY(cudaMemsetAsync(redo_count, 0, sizeof(int), st));
+  VGB_CUDA_TRY(cudaMemsetAsync(redo_count, 0, 3 * sizeof(int), st));
   if (probs) {
     k_clip_site<true, true, SLOTS_FAST, false><<<blocks_for(3), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,

@@ -355,7 +355,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, n_site)) || (rc = dalloc(&e->redo_count, 1)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, n_site)) || (rc = dalloc(&e->redo_count, 3)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
     free_engine(e);

@@ -208,8 +208,9 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* redo_list, int* redo_count,
                     cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
-// reached the security radius.  redo_list (n ints) and redo_count (1 int):
-// cell-tet scratch for the sites a 64-vertex pass hands to a 128-vertex one.
+// reached the security radius.  redo_list (n ints) and redo_count (3 ints:
+// the count, then the two passes' work counters): cell-tet scratch for the
+// sites the first pass hands to the 128-vertex one.
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.
