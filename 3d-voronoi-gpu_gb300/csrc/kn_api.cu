@@ -136,7 +136,7 @@ int kn_solve_ex(kn_problem* kn) {
   if (knn_prepare()) return VGB_ERR_CUDA;
   const ProbDesc lone = lone_problem(kn->allocated_points, kn->dimx, 0, kn->k);
   if (knn_sites(im->sorted, kn->allocated_points, im->cell_start, nullptr, nullptr, lone, kn->k, im->pos_of_id,
-                kn->d_knearests, 0))
+                kn->d_knearests, nullptr, 0))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaStreamSynchronize(0));
   return VGB_OK;

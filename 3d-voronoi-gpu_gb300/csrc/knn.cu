@@ -159,12 +159,23 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
                                                         const int4* __restrict__ tets,
                                                         const int* __restrict__ q_order, int n_query,
                                                         const int* __restrict__ pos_of_id,
-                                                        unsigned* __restrict__ out) {
+                                                        unsigned* __restrict__ out, int* __restrict__ work) {
   __shared__ u64 buf_all[KNN_WARPS][KNN_BUF];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
-  for (int q = blockIdx.x * KNN_WARPS + wib; q < n_query; q += gridDim.x * KNN_WARPS) {
+  // with a work counter, warps draw the next query from it (one wave of
+  // resident blocks: a warp that drew cheap queries takes more); without,
+  // queries are dealt round-robin
+  auto next_q = [&](int cur) {
+    if (work) {
+      int v = 0;
+      if (lane == 0) v = atomicAdd(work, 1);
+      return __shfl_sync(KFULL, v, 0);
+    }
+    return cur + (int)gridDim.x * KNN_WARPS;
+  };
+  for (int q = work ? next_q(0) : blockIdx.x * KNN_WARPS + wib; q < n_query; q = next_q(q)) {
     // centroid queries belong to the lone problem
     int pq = 0;
     const ProbDesc P = CENTROIDS ? lone : prob_for(probs, site_prob, q, lone, pq);
@@ -303,58 +314,61 @@ __global__ void k_pos_of_id(const float4* __restrict__ sites, int n, const ProbD
   pos_of_id[P.site_off + site_id(sites[i])] = i;
 }
 
-static int g_knn_blocks = 0;  // resident CTAs x waves, set by knn_prepare
+static int g_knn_blocks = 0;  // resident CTAs (one wave), set by knn_prepare
 
 int knn_prepare() {
   int dev = 0, sms = 0, per_sm = 0;
   VGB_CUDA_TRY(cudaGetDevice(&dev));
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn<2, false>, KNN_WARPS * 32, 0));
-  g_knn_blocks = sms * (per_sm > 0 ? per_sm : 1) * 8;
+  g_knn_blocks = sms * (per_sm > 0 ? per_sm : 1);
   return 0;
 }
 
 template <bool CENTROIDS>
 static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* site_prob,
                       const ProbDesc& lone, int kmax, int kq, const float4* verts, const int4* tets,
-                      const int* q_order, int n_query, const int* pos_of_id, unsigned* out, cudaStream_t st) {
+                      const int* q_order, int n_query, const int* pos_of_id, unsigned* out, int* work,
+                      cudaStream_t st) {
   if (kmax < 1 || kmax > 128) {
     set_error("kNN: k=%d outside [1, 128]", kmax);
     return -1;
   }
   if (g_knn_blocks == 0 && knn_prepare()) return -1;
   const int need = (n_query + KNN_WARPS - 1) / KNN_WARPS;
-  const int blocks = need < g_knn_blocks ? need : g_knn_blocks;
+  const int want = work ? g_knn_blocks : 8 * g_knn_blocks;  // round-robin: eight waves
+  const int blocks = need < want ? need : want;
+  if (work) VGB_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   if (kmax <= 32)
     k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out);
+                                                           tets, q_order, n_query, pos_of_id, out, work);
   else if (kmax <= 64)
     k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out);
+                                                           tets, q_order, n_query, pos_of_id, out, work);
   else
     k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out);
+                                                           tets, q_order, n_query, pos_of_id, out, work);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, cudaStream_t st) {
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st) {
   if (n <= 0) return 0;
   k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, probs, site_prob, lone, pos_of_id);
   VGB_CUDA_TRY(cudaGetLastError());
   return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kmax, 0, nullptr, nullptr, nullptr, n,
-                           pos_of_id, out, st);
+                           pos_of_id, out, work, st);
 }
 
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
-                      int n_tet, int k, unsigned* out, cudaStream_t st) {
+                      int n_tet, int k, unsigned* out, int* work, cudaStream_t st) {
   (void)tet_cell_start;
   if (n_tet <= 0) return 0;
   const ProbDesc lone = lone_problem(n, dim, n_tet, k);
   return launch_knn<true>(sites, cell_start, nullptr, nullptr, lone, k, k, verts, tets, tet_order, n_tet, pos_of_id,
-                          out, st);
+                          out, work, st);
 }
 
 // ---------------------------------------------------------------------------

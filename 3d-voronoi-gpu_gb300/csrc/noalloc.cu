@@ -117,7 +117,7 @@ extern "C" int vgb_knn_noalloc(const float* d_points, int n, int k, unsigned* d_
   const ProbDesc lone = lone_problem(n, dim, 0, k);
   if (grid_sort(in, sorted, n, (long long)dim * dim * dim, nullptr, nullptr, lone, cell_start, work, st))
     return VGB_ERR_CUDA;
-  if (knn_sites(sorted, n, cell_start, nullptr, nullptr, lone, k, pos_of_id, d_knn, st)) return VGB_ERR_CUDA;
+  if (knn_sites(sorted, n, cell_start, nullptr, nullptr, lone, k, pos_of_id, d_knn, nullptr, st)) return VGB_ERR_CUDA;
   k_na_perm<<<(n + 255) / 256, 256, 0, st>>>(sorted, n, d_perm);
   VGB_CUDA_TRY(cudaGetLastError());
   return VGB_OK;

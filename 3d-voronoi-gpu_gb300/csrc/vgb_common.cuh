@@ -165,10 +165,12 @@ int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbD
 // (lone problem).  Centroid queries come grouped by cell: tet_order /
 // tet_cell_start from tets_by_cell.  kmax: the largest K of the problems.
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, cudaStream_t st);
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st);
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
-                      int n_tet, int k, unsigned* out, cudaStream_t st);
+                      int n_tet, int k, unsigned* out, int* work, cudaStream_t st);
+// work (optional, 1 int): a counter the kNN warps draw queries from (one wave
+// of resident blocks, reset by the call); null deals queries round-robin.
 // Exact form: reach[q] = (distance from the centroid of the q-th tet in
 // centroid-cell order to its nearest site of the same problem) + 2 (its
 // bounding radius); reach_max_bits[p] = float bits of problem p's largest
@@ -208,9 +210,10 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* redo_list, int* redo_count,
                     cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
-// reached the security radius.  redo_list (n ints) and redo_count (3 ints:
-// the count, then the two passes' work counters): cell-tet scratch for the
-// sites the first pass hands to the 128-vertex one.
+// reached the security radius.  redo_list (n ints) and redo_count (at least
+// 3 ints: the count, then the two passes' work counters): cell-tet scratch
+// for the sites the first pass hands to the 128-vertex one.  The engine and
+// the batch keep a fourth int after them for the kNN's work counter.
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.
