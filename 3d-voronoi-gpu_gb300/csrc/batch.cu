@@ -69,7 +69,7 @@ struct vgb_batch {
   unsigned* reach_max = nullptr;
   unsigned* secmiss = nullptr;
   int* redo_list = nullptr;
-  int* redo_count = nullptr;       // redo count, clip and kNN work counters (4)
+  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t tev[2] = {};
 };
@@ -158,7 +158,7 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(b->sites, b->sites_tmp, sizeof(float4) * b->n, cudaMemcpyDeviceToDevice, st));
   if (knn_sites(b->sites, b->n, b->cell_start, b->d_probs, b->site_prob, none, b->kmax, b->pos_of_id, b->knn,
-                b->redo_count + 3, st))
+                b->redo_count + 5, st))
     return VGB_ERR_CUDA;
   if (tet_reach(b->sites, b->cell_start, b->d_probs, b->tet_prob, none, b->n_prob, b->tet_sph, b->n_tet, b->reach,
                 b->reach_max, st))
@@ -341,7 +341,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       (rc = balloc(&b->stats, VGB_STAT_COUNT)) || (rc = balloc(&b->field, f_off)) ||
       (rc = balloc(&b->field_sat, q_off)) || (rc = balloc(&b->reach, b->n_tet)) ||
       (rc = balloc(&b->tet_sph, b->n_tet)) || (rc = balloc(&b->reach_max, n_prob)) ||
-      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, b->n)) || (rc = balloc(&b->redo_count, 4))) {
+      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 2 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 8))) {
     free_batch(b);
     return rc;
   }

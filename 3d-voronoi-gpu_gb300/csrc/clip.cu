@@ -137,7 +137,7 @@ __device__ __forceinline__ void store_master(const WarpCell<SL>& c, SiteSmem<SL>
 //     reached (voronoi.cu:679-697): the cell-tet build and the tet-cell
 //     method's per-tet cells;
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
-template <bool CELL_TET, bool BATCHED, int SL, bool REDO>
+template <bool CELL_TET, bool BATCHED, int SL>
 __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
@@ -145,8 +145,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     dmom4* __restrict__ mom, unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, const int* __restrict__ tet_order,
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
-    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss, int* __restrict__ redo_list,
-    int* __restrict__ redo_count) {
+    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss,
+    const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ out_list,
+    int* __restrict__ out_count, int* __restrict__ work) {
   __shared__ SiteSmem<SL> smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -157,15 +158,12 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   const bool exact = CELL_TET && tet_order != nullptr;
   __syncwarp();
 
-  // REDO: the sites a smaller-capacity pass gave up on (their cell outgrew
-  // it); otherwise every site, and a site that outgrows the capacity is
-  // handed on through redo_list when there is one.  With redo_count given,
-  // warps take the next item from a counter (redo_count[1] for the first
-  // pass, [2] for the redo pass) in a single wave of resident blocks, so a
-  // warp that drew cheap sites takes more; the tet-cell method deals items
-  // round-robin.
-  const int n_items = REDO ? *redo_count : n;
-  int* const work = redo_count ? redo_count + (REDO ? 2 : 1) : nullptr;
+  // The sites in_list names (in_count of them), or every site.  A site whose
+  // cell outgrows the capacity is handed on through out_list when there is
+  // one (else its clip is dropped and counted).  With a work counter, warps
+  // take the next item from it in a single wave of resident blocks, so a warp
+  // that drew cheap sites takes more; without, items are dealt round-robin.
+  const int n_items = in_list ? *in_count : n;
   auto next_item = [&](int cur) {
     if (work) {
       int v = 0;
@@ -175,7 +173,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     return cur + (int)gridDim.x * CLIP_WARPS;
   };
   for (int it = work ? next_item(0) : blockIdx.x * CLIP_WARPS + wib; it < n_items; it = next_item(it)) {
-    const int s = REDO ? redo_list[it] : it;
+    const int s = in_list ? in_list[it] : it;
     bool abandon = false;
     // the site's problem; its descriptor fields are read where used (from
     // global memory or the kernel parameters) rather than held in registers
@@ -428,7 +426,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         seq_cnt += 1u + ((unsigned)c.nt << 16);
         const int r = warp_clip(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane, need_r2);
         if (r == CLIP_EMPTY) { state = 1; break; }
-        if (!REDO && r == CLIP_OVERFLOW && redo_list) {
+        if (r == CLIP_OVERFLOW && out_list) {
           abandon = true;
           break;
         }
@@ -593,7 +591,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     if (abandon) {
       // the larger-capacity pass redoes this site from scratch
       if (lane == 0) {
-        redo_list[atomicAdd(redo_count, 1)] = s;
+        out_list[atomicAdd(out_count, 1)] = s;
         S.cnt[WC_REDO]++;
       }
       __syncwarp();
@@ -615,14 +613,204 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   }
 }
 
-// Cell capacity (triangle slots per lane): the cell-tet form runs with 2
-// (64 vertices) and redoes the rare sites whose cell outgrows it with 4 (128);
-// the tet-cell method runs with 3 (96, the reference's capacity).
+// Shared state of one lane group of k_build: the site's bisector and
+// start-cube planes, and its clip scratch.
+template <int CAP>
+struct BuildSmem {
+  float4 plane[4 + MAX_SITE_K + BOX_PLANES];  // 4+j bisector j, 4+K+b start-cube face b
+  unsigned conf[CAP];
+  unsigned bedge[CAP];
+  unsigned cnt[WC_N];
+};
+
+// First pass of the exact cell-tet form: WARP / G sites per warp, one per
+// group of G lanes, each group building its site's cell from the bisectors
+// exactly as k_clip_site does (the same start cube, plane order and security
+// test).  A cell that provably lies inside the mesh is taken whole and its
+// moments written; every other site -- a boundary cell, a cell that missed
+// its security radius, failed, or outgrew G SL vertices -- goes on out_list
+// for k_clip_site, which starts it again.  Groups draw sites from the work
+// counter independently; a warp's groups run one instruction stream, a
+// group whose cell is done passing its turn in each clip.
+template <bool BATCHED, int G, int SL>
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
+    const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
+    const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
+    unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
+    const unsigned* __restrict__ field_sat, int* __restrict__ work, int* __restrict__ out_list,
+    int* __restrict__ out_count) {
+  constexpr int NG = WARP / G;
+  __shared__ BuildSmem<G * SL> smem_all[CLIP_WARPS * NG];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gid = lane / G, gl = lane % G, gbase = gid * G;
+  const unsigned lb = 1u << gl;
+  BuildSmem<G * SL>& S = smem_all[wib * NG + gid];
+  for (int i = gl; i < WC_N; i += G) S.cnt[i] = 0u;
+  __syncwarp();
+
+  while (true) {
+    int v = 0;
+    if (gl == 0) v = atomicAdd(work, 1);
+    const int s = __shfl_sync(FULL, v, gbase);
+    const bool has = s < n;
+    if (!__any_sync(FULL, has)) break;
+    const int pidx = (BATCHED && has) ? site_prob[s] : 0;
+#define PD(f) (BATCHED ? probs[pidx].f : lone.f)
+    const int K = has ? PD(K) : 0;
+    const float4 seed = has ? sites[s] : make_float4(500.f, 500.f, 500.f, 0.f);
+    // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
+    if (has) {
+      const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
+      for (int j = gl; j < K; j += G) {
+        const float4 B = sites[krow[j]];
+        const float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
+        const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
+        S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
+      }
+    }
+    // the start cube centred on the site, containing the domain box
+    constexpr float lo = -0.1f, hi = 1000.1f;
+    const float L = fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
+                          fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
+    if (gl < BOX_PLANES) {
+      const int ax = gl >> 1;
+      const float sgn = (gl & 1) ? -1.f : 1.f;
+      S.plane[4 + K + gl] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
+    }
+    __syncwarp();
+    WarpCell<SL> c;
+    cell_clear(c);
+    if (has && gl < 8) {
+      const unsigned bx = gl & 1, by = (gl >> 1) & 1, bz = (gl >> 2) & 1;
+      const unsigned fx = 4 + K + bx, fy = 4 + K + 2 + by, fz = 4 + K + 4 + bz;
+      c.tri[0] = ((bx ^ by ^ bz) & 1) ? pack_tri(fx, fy, fz) : pack_tri(fx, fz, fy);
+      c.vx[0] = bx ? L : -L;
+      c.vy[0] = by ? L : -L;
+      c.vz[0] = bz ? L : -L;
+      c.vw[0] = 3.f * L * L;
+    }
+    c.vm[0] = has ? 0xffu : 0u;
+    c.nt = has ? 8 : 0;
+    c.r2 = 3.f * L * L;
+
+    // bisectors, nearest first, until the security radius
+    bool building = has, secmiss = true;
+    int pi = 4, state = 0;
+    const int pend = 4 + K;
+    unsigned seq_cnt = 0u;  // planes (bits 0-7), cuts (8-15), vertex-vs-plane tests (16-31)
+    while (__any_sync(FULL, building)) {
+      const float4 P = building ? S.plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
+      if (building) seq_cnt += 1u + ((unsigned)c.nt << 16);
+      const int r = group_clip<G, SL>(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, gl, gbase, gid, building);
+      if (building) {
+        if (r == CLIP_EMPTY) {
+          state = 1;
+          building = false;
+        } else if (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY) {
+          state = 2;
+          building = false;
+        } else {
+          if (r == CLIP_CUT) seq_cnt += 1u << 8;
+          // |neighbour - site|^2 > 4 max|v - site|^2
+          if (2.f * P.w > 4.f * c.r2) {
+            secmiss = false;
+            building = false;
+          } else if (++pi == pend) {
+            building = false;
+          }
+        }
+      }
+    }
+
+    // inside the mesh: the site cell's clear radius against the ball of
+    // radius Rc, then the cell's vertex box against the summed table (the
+    // test of k_clip_site)
+    const bool built = has && state == 0 && !secmiss;
+    const float Rc = sqrtf(c.r2);
+    const float Rq = Rc * 1.001f + 0.01f;
+    const int fdim = field ? PD(fdim) : 1;
+    const int fv = built && field && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f && seed.y <= 1000.f &&
+                           seed.z >= 0.f && seed.z <= 1000.f
+                       ? field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]
+                       : 0;
+    bool interior = false;
+    if (fv && seed.x - Rq >= 0.f && seed.x + Rq <= 1000.f && seed.y - Rq >= 0.f && seed.y + Rq <= 1000.f &&
+        seed.z - Rq >= 0.f && seed.z + Rq <= 1000.f) {
+      const int ci = grid_axis(seed.x, fdim), cj = grid_axis(seed.y, fdim), ck = grid_axis(seed.z, fdim);
+      const int need = max(max(max(ci - grid_axis(seed.x - Rq, fdim), grid_axis(seed.x + Rq, fdim) - ci),
+                               max(cj - grid_axis(seed.y - Rq, fdim), grid_axis(seed.y + Rq, fdim) - cj)),
+                           max(ck - grid_axis(seed.z - Rq, fdim), grid_axis(seed.z + Rq, fdim) - ck));
+      interior = need < fv;
+    }
+    const bool need_box = fv && !interior;
+    if (__any_sync(FULL, need_box)) {
+      float l0 = FLT_MAX, l1 = FLT_MAX, l2 = FLT_MAX, h0 = -FLT_MAX, h1 = -FLT_MAX, h2 = -FLT_MAX;
+#pragma unroll
+      for (int k = 0; k < SL; ++k)
+        if (c.vm[k] & lb) {
+          l0 = fminf(l0, c.vx[k]); h0 = fmaxf(h0, c.vx[k]);
+          l1 = fminf(l1, c.vy[k]); h1 = fmaxf(h1, c.vy[k]);
+          l2 = fminf(l2, c.vz[k]); h2 = fmaxf(h2, c.vz[k]);
+        }
+      const float lo0 = ord_val(group_min_u<G>(ord_key(l0), gid)), lo1 = ord_val(group_min_u<G>(ord_key(l1), gid)),
+                  lo2 = ord_val(group_min_u<G>(ord_key(l2), gid));
+      const float hi0 = ord_val(group_max_u<G>(ord_key(h0), gid)), hi1 = ord_val(group_max_u<G>(ord_key(h1), gid)),
+                  hi2 = ord_val(group_max_u<G>(ord_key(h2), gid));
+      const float m = 1e-3f * Rc + 0.01f;
+      const float x0 = seed.x + lo0 - m, x1 = seed.x + hi0 + m, y0 = seed.y + lo1 - m, y1 = seed.y + hi1 + m,
+                  z0 = seed.z + lo2 - m, z1 = seed.z + hi2 + m;
+      if (need_box && x0 >= 0.f && x1 <= 1000.f && y0 >= 0.f && y1 <= 1000.f && z0 >= 0.f && z1 <= 1000.f) {
+        const int a0 = grid_axis(x0, fdim), a1 = grid_axis(x1, fdim) + 1;
+        const int b0 = grid_axis(y0, fdim), b1 = grid_axis(y1, fdim) + 1;
+        const int c0 = grid_axis(z0, fdim), c1 = grid_axis(z1, fdim) + 1;
+        const size_t W = (size_t)fdim + 1;
+        const unsigned* sat = field_sat + PD(sat_off);
+        auto at = [&](int i, int j, int k) { return __ldg(sat + (size_t)i + W * ((size_t)j + W * (size_t)k)); };
+        const unsigned touched = at(a1, b1, c1) - at(a0, b1, c1) - at(a1, b0, c1) - at(a1, b1, c0) +
+                                 at(a0, b0, c1) + at(a0, b1, c0) + at(a1, b0, c0) - at(a0, b0, c0);
+        interior = touched == 0u;
+      }
+    }
+    if (__any_sync(FULL, interior)) {
+      float vol, mx, my, mz;
+      group_moments<G, SL>(c, S.plane, gl, vol, mx, my, mz);
+      if (interior && gl == 0) {
+        mom[s] = make_dmom4((double)vol, (double)mx, (double)my, (double)mz);
+        S.cnt[WC_INTERIOR]++;
+        S.cnt[WC_FINAL] += (unsigned)c.nt;
+      }
+    }
+    if (has && gl == 0) {
+      S.cnt[WC_PLANES] += seq_cnt & 0xffu;
+      S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
+      S.cnt[WC_CONFLICT] += seq_cnt >> 16;
+      if (!interior) out_list[atomicAdd(out_count, 1)] = s;
+    }
+    __syncwarp();
+#undef PD
+  }
+  if (stats) {
+    static const int slot[WC_N] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB,
+                                   STAT_SECURITY_MISS, STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES,
+                                   STAT_CLIPS, STAT_FINAL_VERTICES, STAT_CONFLICT_TESTS, STAT_CULL_TESTS,
+                                   STAT_NEW_VERTICES, STAT_INTERIOR, STAT_REDO};
+    for (int i = gl; i < WC_N; i += G)
+      if (S.cnt[i]) atomicAdd(stats + slot[i], (unsigned long long)S.cnt[i]);
+  }
+}
+
+// Cell capacity (triangle slots per lane): the exact cell-tet form builds
+// every cell in lane groups of 16 with 2 slots (32 vertices) and finishes the
+// inside cells there; the other sites run one warp each with 2 slots (64
+// vertices), and the rare sites whose cell outgrows that with 4 (128).  The
+// reference cell-tet form starts at the one-warp pass.  The tet-cell method
+// runs with 3 (96, the reference's capacity).
+constexpr int BUILD_G = 16, BUILD_SL = 2;
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
 
 // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
-// fast / redo, cell-tet batched fast / redo
-static int g_clip_resident_blocks[5] = {0, 0, 0, 0, 0};
+// fast / redo, cell-tet batched fast / redo, first pass lone / batched
+static int g_clip_resident_blocks[7] = {0, 0, 0, 0, 0, 0, 0};
 
 template <class F>
 static int resident_blocks(F kernel, int sms, int* out) {
@@ -637,11 +825,13 @@ int clip_prepare() {
   VGB_CUDA_TRY(cudaGetDevice(&dev));
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int* r = g_clip_resident_blocks;
-  if (resident_blocks(k_clip_site<false, false, SLOTS_TET_CELL, false>, sms, r + 0) ||
-      resident_blocks(k_clip_site<true, false, SLOTS_FAST, false>, sms, r + 1) ||
-      resident_blocks(k_clip_site<true, false, SLOTS_REDO, true>, sms, r + 2) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_FAST, false>, sms, r + 3) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_REDO, true>, sms, r + 4))
+  if (resident_blocks(k_clip_site<false, false, SLOTS_TET_CELL>, sms, r + 0) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_FAST>, sms, r + 1) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_REDO>, sms, r + 2) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_FAST>, sms, r + 3) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_REDO>, sms, r + 4) ||
+      resident_blocks(k_build<false, BUILD_G, BUILD_SL>, sms, r + 5) ||
+      resident_blocks(k_build<true, BUILD_G, BUILD_SL>, sms, r + 6))
     return -2;
   return 0;
 }
@@ -651,7 +841,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* redo_list, int* redo_count,
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters,
                     cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
@@ -659,39 +849,50 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     set_error("the tet-cell method runs one problem at a time");
     return -1;
   }
-  if (cell_tet && !redo_list) {
-    set_error("the cell-tet clip needs its redo list");
+  if (cell_tet && (!lists || !counters)) {
+    set_error("the cell-tet clip needs its site lists and counters");
     return -1;
   }
-  // the cell-tet passes: one wave of resident blocks whose warps draw sites
-  // from a counter; the tet-cell method: a few waves, sites dealt round-robin
-  auto blocks_for = [&](int variant) {
-    const long long want = (long long)g_clip_resident_blocks[variant] * (variant == 0 ? 4 : 1);
-    const long long need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
-    return (int)(want < need ? want : need);
-  };
   if (!cell_tet) {
-    k_clip_site<false, false, SLOTS_TET_CELL, false><<<blocks_for(0), CLIP_WARPS * WARP, 0, st>>>(
+    // a few waves of resident blocks, sites dealt round-robin
+    const long long want = (long long)g_clip_resident_blocks[0] * 4, need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
+    k_clip_site<false, false, SLOTS_TET_CELL><<<(int)(want < need ? want : need), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
-        nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr);
+        nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr);
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
-  VGB_CUDA_TRY(cudaMemsetAsync(redo_count, 0, 3 * sizeof(int), st));
+  // counters: [0] sites the first pass hands on, [1] sites the one-warp pass
+  // hands on, [2..4] the three passes' work counters; lists: [0, n) the
+  // one-warp pass's hand-offs, [n, 2n) the first pass's
+  const bool exact = tet_order != nullptr;
+  int* const redo = lists;
+  int* const rest = lists + n;
+  VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 5 * sizeof(int), st));
+  // every pass: one wave of resident blocks whose warps draw sites from a counter
+  auto launch = [&](auto kernel, int variant, const int* in_list, const int* in_count, int* out_list, int* out_count,
+                    int* work) {
+    kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
+        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
+        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, in_list, in_count, out_list,
+        out_count, work);
+  };
+  if (exact) {
+    if (probs)
+      k_build<true, BUILD_G, BUILD_SL><<<g_clip_resident_blocks[6], CLIP_WARPS * WARP, 0, st>>>(
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0);
+    else
+      k_build<false, BUILD_G, BUILD_SL><<<g_clip_resident_blocks[5], CLIP_WARPS * WARP, 0, st>>>(
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0);
+  }
+  const int* in_list = exact ? rest : nullptr;
+  const int* in_count = exact ? counters + 0 : nullptr;
   if (probs) {
-    k_clip_site<true, true, SLOTS_FAST, false><<<blocks_for(3), CLIP_WARPS * WARP, 0, st>>>(
-        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
-        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
-    k_clip_site<true, true, SLOTS_REDO, true><<<g_clip_resident_blocks[4], CLIP_WARPS * WARP, 0, st>>>(
-        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
-        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+    launch(k_clip_site<true, true, SLOTS_FAST>, 3, in_list, in_count, redo, counters + 1, counters + 3);
+    launch(k_clip_site<true, true, SLOTS_REDO>, 4, redo, counters + 1, nullptr, nullptr, counters + 4);
   } else {
-    k_clip_site<true, false, SLOTS_FAST, false><<<blocks_for(1), CLIP_WARPS * WARP, 0, st>>>(
-        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
-        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
-    k_clip_site<true, false, SLOTS_REDO, true><<<g_clip_resident_blocks[2], CLIP_WARPS * WARP, 0, st>>>(
-        sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
-        tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, redo_list, redo_count);
+    launch(k_clip_site<true, false, SLOTS_FAST>, 1, in_list, in_count, redo, counters + 1, counters + 3);
+    launch(k_clip_site<true, false, SLOTS_REDO>, 2, redo, counters + 1, nullptr, nullptr, counters + 4);
   }
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;

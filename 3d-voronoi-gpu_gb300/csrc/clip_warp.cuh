@@ -327,4 +327,225 @@ __device__ __forceinline__ void warp_moments(const WarpCell<SL>& c, const float4
   mz = fmaf(warp_sum(lmz), 1.f / 24.f, vol * cz);
 }
 
+// ---------------------------------------------------------------------------
+// Lane groups: the warp split into 32 / G groups of G lanes, one cell per
+// group, slot (k, lane) of a group's cell live when bit `gl` (the lane's
+// index in its group) of vm[k] is set.  Every collective below is executed
+// by the whole warp at once, each group reading its own part, so groups
+// whose cells are in different states still run one instruction stream: a
+// group with nothing to do passes its turn with act = false.
+// ---------------------------------------------------------------------------
+
+// The low G bits.
+template <int G>
+__host__ __device__ constexpr unsigned group_bits() {
+  return G >= 32 ? 0xffffffffu : ((1u << (G & 31)) - 1u);
+}
+
+// A group's bits of a warp ballot.
+template <int G>
+__device__ __forceinline__ unsigned group_ballot(bool p, int gbase) {
+  const unsigned b = __ballot_sync(FULL, p);
+  return G == WARP ? b : (b >> gbase) & group_bits<G>();
+}
+
+template <int G>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+// Largest / smallest of one unsigned per lane over the group: one warp
+// reduction per group, each lane keeping its own group's result.
+template <int G>
+__device__ __forceinline__ unsigned group_max_u(unsigned v, int gid) {
+  if (G == WARP) return __reduce_max_sync(FULL, v);
+  unsigned r = 0u;
+#pragma unroll
+  for (int g = 0; g < WARP / G; ++g) {
+    const unsigned x = __reduce_max_sync(FULL, gid == g ? v : 0u);
+    if (gid == g) r = x;
+  }
+  return r;
+}
+template <int G>
+__device__ __forceinline__ unsigned group_min_u(unsigned v, int gid) {
+  if (G == WARP) return __reduce_min_sync(FULL, v);
+  unsigned r = 0u;
+#pragma unroll
+  for (int g = 0; g < WARP / G; ++g) {
+    const unsigned x = __reduce_min_sync(FULL, gid == g ? v : 0xffffffffu);
+    if (gid == g) r = x;
+  }
+  return r;
+}
+
+// warp_clip for the cell of a lane group (act: this group clips; the others
+// only take part in the collectives).  The same steps: remove the vertices
+// strictly outside P; a directed edge of a removed triangle is on the
+// cavity boundary when no removed triangle holds its twin (each edge lane
+// searches the group's removed triangles); each boundary vertex must start
+// and end exactly one boundary edge; the fan (pidx, a, b) fills freed slots.
+// Returns the group's result; the cell is changed only on CLIP_CUT.  conf and
+// bedge: the group's G SL-entry scratch arrays.
+template <int G, int SL>
+__device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
+                                          unsigned* conf, unsigned* bedge, const int gl, const int gbase,
+                                          const int gid, const bool act) {
+  constexpr int CAP = G * SL;
+  const unsigned lb = 1u << gl, ltm = lb - 1u;
+  unsigned m[SL];
+  int nconf = 0;
+#pragma unroll
+  for (int k = 0; k < SL; ++k) {
+    const bool cf = act && (c.vm[k] & lb) && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
+    m[k] = group_ballot<G>(cf, gbase);
+    nconf += __popc(m[k]);
+  }
+  const bool cut = act && nconf > 0 && nconf < c.nt;
+  int res = (!act || nconf == 0) ? CLIP_NONE : nconf == c.nt ? CLIP_EMPTY : CLIP_CUT;
+  if (!__any_sync(FULL, cut)) return res;
+  const int R = cut ? nconf : 0;
+  {
+    int off = 0;
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+      if (cut && (m[k] & lb)) conf[off + __popc(m[k] & ltm)] = c.tri[k];
+      off += __popc(m[k]);
+    }
+  }
+  __syncwarp();
+  // boundary edges, G at a time
+  const int E = 3 * R;
+  const int Emax = (int)__reduce_max_sync(FULL, (unsigned)E);
+  int nb = 0;
+  for (int e0 = 0; e0 < Emax; e0 += G) {
+    const int e = e0 + gl;
+    bool isb = false;
+    unsigned ea = 0, eb = 0;
+    if (e < E) {
+      const unsigned T = conf[e / 3];
+      const int es = e % 3;
+      ea = tri_at(T, es);
+      eb = tri_at(T, es == 2 ? 0 : es + 1);
+      // the twin (eb -> ea) as a directed-edge code lo | hi << 8; the codes
+      // of U = (u0, u1, u2) are its bytes 0-1, 1-2 and 2-0
+      const unsigned tw = eb | (ea << 8);
+      bool twin = false;
+      for (int q = 0; q < R; ++q) {
+        const unsigned U = conf[q];
+        twin |= ((U & 0xffffu) == tw) | (((U >> 8) & 0xffffu) == tw) | (__byte_perm(U, 0u, 0x4402u) == tw);
+      }
+      isb = !twin;
+    }
+    const unsigned bm = group_ballot<G>(isb, gbase);
+    if (isb) {
+      const int r = nb + __popc(bm & ltm);
+      if (r < CAP) bedge[r] = ea | (eb << 8);
+    }
+    nb += __popc(bm);
+  }
+  __syncwarp();
+  // each boundary vertex starts exactly one edge and ends exactly one
+  const int nbc = (cut && nb <= CAP) ? nb : 0;
+  const int NBmax = (int)__reduce_max_sync(FULL, (unsigned)nbc);
+  bool bad = false;
+  for (int e0 = 0; e0 < NBmax; e0 += G) {
+    const int e = e0 + gl;
+    if (e < nbc) {
+      const unsigned Ed = bedge[e];
+      int starts = 0, ends = 0;
+      for (int q = 0; q < nbc; ++q) {
+        const unsigned F = bedge[q];
+        starts += (F & 0xffu) == (Ed & 0xffu);
+        ends += (F >> 8) == (Ed >> 8);
+      }
+      bad |= starts != 1 || ends != 1;
+    }
+  }
+  bad = group_ballot<G>(bad, gbase) != 0u;
+  const int nt2 = c.nt - R + nb;
+  if (cut) {
+    if (nt2 > CAP) res = CLIP_OVERFLOW;
+    else if (bad || nb < 3) res = CLIP_BOUNDARY;
+  }
+  const bool place = res == CLIP_CUT;
+  __syncwarp();
+  float lm = 0.f;
+  int base = 0;
+  bool nonfinite = false;
+  unsigned vm2[SL];
+#pragma unroll
+  for (int k = 0; k < SL; ++k) {
+    const unsigned keep = place ? (c.vm[k] & ~m[k]) : c.vm[k];
+    const unsigned freem = ~keep & group_bits<G>();
+    const int r = base + __popc(freem & ltm);
+    const bool recv = place && (freem & lb) && r < nb;
+    if (recv) {
+      const unsigned Ed = bedge[r];
+      const unsigned ea = Ed & 0xffu, eb = Ed >> 8;
+      const float3 x = vertex_of(P, planes[ea], planes[eb]);
+      c.tri[k] = pack_tri(pidx, ea, eb);
+      c.vx[k] = x.x;
+      c.vy[k] = x.y;
+      c.vz[k] = x.z;
+      c.vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
+      nonfinite |= !isfinite(c.vw[k]);
+    }
+    vm2[k] = keep | group_ballot<G>(recv, gbase);
+    base += __popc(freem);
+    if (vm2[k] & lb) lm = fmaxf(lm, c.vw[k]);
+  }
+  // a new vertex from (nearly) parallel planes: the conflict decisions were
+  // inconsistent (a plane through an edge, within rounding); drop the cell
+  const bool nf = group_ballot<G>(nonfinite, gbase) != 0u;
+  const float r2 = __uint_as_float(group_max_u<G>(__float_as_uint(lm), gid));
+  if (place) {
+#pragma unroll
+    for (int k = 0; k < SL; ++k) c.vm[k] = vm2[k];
+    c.nt = nt2;
+    c.r2 = r2;
+    if (nf) res = CLIP_BOUNDARY;
+  }
+  __syncwarp();
+  return res;
+}
+
+// warp_moments over a lane group's cell (every group takes part; the values
+// of a group with no cell are meaningless).
+template <int G, int SL>
+__device__ __forceinline__ void group_moments(const WarpCell<SL>& c, const float4* planes, const int gl, float& vol,
+                                              float& mx, float& my, float& mz) {
+  const unsigned lb = 1u << gl;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+  for (int k = 0; k < SL; ++k)
+    if (c.vm[k] & lb) { sx += c.vx[k]; sy += c.vy[k]; sz += c.vz[k]; }
+  const float inv = __frcp_rn((float)max(c.nt, 1));
+  const float cx = group_sum<G>(sx) * inv, cy = group_sum<G>(sy) * inv, cz = group_sum<G>(sz) * inv;
+  float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
+#pragma unroll
+  for (int k = 0; k < SL; ++k) {
+    if (c.vm[k] & lb) {
+      const unsigned T = c.tri[k];
+      float4 q0 = planes[tri_at(T, 0)], q1 = planes[tri_at(T, 1)], q2 = planes[tri_at(T, 2)];
+      q0.w += q0.x * cx + q0.y * cy + q0.z * cz;  // planes relative to the apex
+      q1.w += q1.x * cx + q1.y * cy + q1.z * cz;
+      q2.w += q2.x * cx + q2.y * cy + q2.z * cz;
+      float v6;
+      float3 m24;
+      vertex_moments(make_float3(c.vx[k] - cx, c.vy[k] - cy, c.vz[k] - cz), q0, q1, q2, v6, m24);
+      lv += v6;
+      lmx += m24.x;
+      lmy += m24.y;
+      lmz += m24.z;
+    }
+  }
+  vol = group_sum<G>(lv) * (1.f / 6.f);
+  mx = fmaf(group_sum<G>(lmx), 1.f / 24.f, vol * cx);
+  my = fmaf(group_sum<G>(lmy), 1.f / 24.f, vol * cy);
+  mz = fmaf(group_sum<G>(lmz), 1.f / 24.f, vol * cz);
+}
+
 }  // namespace vgb

@@ -58,8 +58,8 @@ struct vgb_engine {
   float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
   float4* tet_sph = nullptr;       // exact form: tet bounding spheres (centroid-cell order)
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
-  int* redo_list = nullptr;        // cell-tet: sites handed from the 64- to the 128-vertex pass (n)
-  int* redo_count = nullptr;       // redo count, clip and kNN work counters (4)
+  int* redo_list = nullptr;        // cell-tet: sites handed from one clip pass to the next (2n)
+  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -190,7 +190,7 @@ int run_pass(vgb_engine* e, int update) {
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(e->sites, e->sites_tmp, sizeof(float4) * e->n, cudaMemcpyDeviceToDevice, st));
   MARK(1);
-  if (knn_sites(e->sites, e->n, e->cell_start, nullptr, nullptr, e->prob, e->K, e->pos_of_id, e->knn, e->redo_count + 3,
+  if (knn_sites(e->sites, e->n, e->cell_start, nullptr, nullptr, e->prob, e->K, e->pos_of_id, e->knn, e->redo_count + 5,
                 st))
     return VGB_ERR_CUDA;
   MARK(2);
@@ -200,7 +200,7 @@ int run_pass(vgb_engine* e, int update) {
     return VGB_ERR_CUDA;
   if (!exact &&
       knn_tet_centroids(e->sites, e->n, e->dim, e->cell_start, e->pos_of_id, e->verts, e->tets, e->tet_order,
-                        e->tet_cell_start, e->n_tet, e->tk, e->cand, e->redo_count + 3, st))
+                        e->tet_cell_start, e->n_tet, e->tk, e->cand, e->redo_count + 5, st))
     return VGB_ERR_CUDA;
   MARK(3);
   if (!exact && e->cfg.method != VGB_METHOD_PLAIN) {
@@ -356,7 +356,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, n_site)) || (rc = dalloc(&e->redo_count, 4)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 2 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 8)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
     free_engine(e);
