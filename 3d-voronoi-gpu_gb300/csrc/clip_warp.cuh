@@ -101,6 +101,16 @@ __device__ __forceinline__ void cell_clear(WarpCell<SL>& c) {
   c.r2 = 0.f;
 }
 
+// The removed triangles of a clip form a disk (the cavity) exactly when its
+// boundary edges make one simple loop.  Their boundary is a cycle, so every
+// vertex ends as many boundary edges as it starts, and checking that none
+// starts two covers both.  A cavity of R <= 3 triangles needs no edge-by-edge
+// check: it is a disk exactly when it has R + 2 boundary edges (one, two or
+// three triangles in a strip) or three (three triangles around one vertex,
+// a face of the cell that disappears); any other arrangement of so few
+// triangles (pinched at a vertex, or in pieces) has more.
+__device__ __forceinline__ bool cavity_disk_small(int R, int nb) { return nb == R + 2 || (R == 3 && nb == 3); }
+
 // Clip the cell by plane P (id pidx): remove the vertices strictly outside,
 // then close the cavity with the fan (pidx, a, b) over its boundary edges
 // (a -> b).  The reference finds the boundary by walking the removed
@@ -111,7 +121,8 @@ __device__ __forceinline__ void cell_clear(WarpCell<SL>& c) {
 // ten triangles).  Each boundary vertex must start and end exactly one
 // boundary edge, else the cell is dropped (the reference's
 // inconsistent_boundary).  New triangles fill freed slots; the receiving lane
-// computes the new vertex.  conf and bedge are 32 SL-entry scratch arrays of
+// computes the new vertex (the loop test: cavity_disk_small).  conf and
+// bedge are 32 SL-entry scratch arrays of
 // the warp.  need_r2: keep c.r2 (the largest |vertex|^2) current; callers that
 // never read it skip the warp reduction.
 template <int SL>
@@ -159,10 +170,13 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
     const bool isb = live && __popc(same) == 1;
     const unsigned bm = __ballot_sync(FULL, isb);
     nb = __popc(bm);
-    const unsigned ka = isb ? ea : (0x20000u | lane), kb = isb ? eb : (0x30000u | lane);
-    const unsigned ga = __match_any_sync(FULL, ka);
-    const unsigned gb = __match_any_sync(FULL, kb);
-    bad = __any_sync(FULL, isb && (__popc(ga) != 1 || __popc(gb) != 1));
+    if (R <= 3) {
+      bad = !cavity_disk_small(R, nb);
+    } else {
+      const unsigned ka = isb ? ea : (0x20000u | lane);
+      const unsigned ga = __match_any_sync(FULL, ka);
+      bad = __any_sync(FULL, isb && __popc(ga) != 1);
+    }
     if (isb) bedge[__popc(bm & lt_mask)] = ea | (eb << 8);
   } else {
     for (int e0 = 0; e0 < 3 * R; e0 += WARP) {
@@ -193,23 +207,18 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
     }
     __syncwarp();
     if (nb <= WARP) {
-      // each boundary vertex starts exactly one edge and ends exactly one
+      // each boundary vertex starts exactly one edge
       const bool live = lane < nb;
       const unsigned E = live ? bedge[lane] : 0u;
-      const unsigned ka = live ? (E & 0xffu) : (0x20000u | lane), kb = live ? (E >> 8) : (0x30000u | lane);
+      const unsigned ka = live ? (E & 0xffu) : (0x20000u | lane);
       const unsigned ga = __match_any_sync(FULL, ka);
-      const unsigned gb = __match_any_sync(FULL, kb);
-      bad = live && (__popc(ga) != 1 || __popc(gb) != 1);
+      bad = live && __popc(ga) != 1;
     } else if (nb <= (WARP * SL)) {
       for (int e = lane; e < nb; e += WARP) {
         unsigned E = bedge[e];
-        int starts = 0, ends = 0;
-        for (int q = 0; q < nb; ++q) {
-          unsigned F = bedge[q];
-          starts += (F & 0xffu) == (E & 0xffu);
-          ends += (F >> 8) == (E >> 8);
-        }
-        if (starts != 1 || ends != 1) bad = true;
+        int starts = 0;
+        for (int q = 0; q < nb; ++q) starts += (bedge[q] & 0xffu) == (E & 0xffu);
+        if (starts != 1) bad = true;
       }
     }
     bad = __any_sync(FULL, bad);
@@ -447,24 +456,22 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
     nb += __popc(bm);
   }
   __syncwarp();
-  // each boundary vertex starts exactly one edge and ends exactly one
-  const int nbc = (cut && nb <= CAP) ? nb : 0;
+  // a cavity of at most three triangles by its edge count; a larger one
+  // edge by edge: each boundary vertex starts exactly one edge
+  const int nbc = (cut && R > 3 && nb <= CAP) ? nb : 0;
   const int NBmax = (int)__reduce_max_sync(FULL, (unsigned)nbc);
   bool bad = false;
   for (int e0 = 0; e0 < NBmax; e0 += G) {
     const int e = e0 + gl;
     if (e < nbc) {
       const unsigned Ed = bedge[e];
-      int starts = 0, ends = 0;
-      for (int q = 0; q < nbc; ++q) {
-        const unsigned F = bedge[q];
-        starts += (F & 0xffu) == (Ed & 0xffu);
-        ends += (F >> 8) == (Ed >> 8);
-      }
-      bad |= starts != 1 || ends != 1;
+      int starts = 0;
+      for (int q = 0; q < nbc; ++q) starts += (bedge[q] & 0xffu) == (Ed & 0xffu);
+      bad |= starts != 1;
     }
   }
   bad = group_ballot<G>(bad, gbase) != 0u;
+  if (cut && R <= 3) bad = !cavity_disk_small(R, nb);
   const int nt2 = c.nt - R + nb;
   if (cut) {
     if (nt2 > CAP) res = CLIP_OVERFLOW;
