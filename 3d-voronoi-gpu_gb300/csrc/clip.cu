@@ -800,12 +800,12 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
 }
 
 // Cell capacity (triangle slots per lane): the exact cell-tet form builds
-// every cell in lane groups of 16 with 2 slots (32 vertices) and finishes the
-// inside cells there; the other sites run one warp each with 2 slots (64
+// every cell in lane groups of 8 with 4 slots (32 vertices, four sites per
+// warp) and finishes the inside cells there; the other sites run one warp each with 2 slots (64
 // vertices), and the rare sites whose cell outgrows that with 4 (128).  The
 // reference cell-tet form starts at the one-warp pass.  The tet-cell method
 // runs with 3 (96, the reference's capacity).
-constexpr int BUILD_G = 16, BUILD_SL = 2;
+constexpr int BUILD_G = 8, BUILD_SL = 4;
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
 
 // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone

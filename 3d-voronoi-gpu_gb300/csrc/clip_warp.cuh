@@ -378,6 +378,15 @@ __device__ __forceinline__ unsigned group_max_u(unsigned v, int gid) {
   }
   return r;
 }
+// Largest of one non-negative float per lane over the group.
+template <int G>
+__device__ __forceinline__ float group_max_nonneg(float v, int gid) {
+  if (G == WARP) return __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(v)));
+  (void)gid;
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
 template <int G>
 __device__ __forceinline__ unsigned group_min_u(unsigned v, int gid) {
   if (G == WARP) return __reduce_min_sync(FULL, v);
@@ -406,11 +415,14 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
   const unsigned lb = 1u << gl, ltm = lb - 1u;
   unsigned m[SL];
   int nconf = 0;
+  float lm = 0.f;  // largest |v|^2 of the vertices kept
 #pragma unroll
   for (int k = 0; k < SL; ++k) {
-    const bool cf = act && (c.vm[k] & lb) && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
+    const bool live = c.vm[k] & lb;
+    const bool cf = act && live && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
     m[k] = group_ballot<G>(cf, gbase);
     nconf += __popc(m[k]);
+    if (live && !cf) lm = fmaxf(lm, c.vw[k]);
   }
   const bool cut = act && nconf > 0 && nconf < c.nt;
   int res = (!act || nconf == 0) ? CLIP_NONE : nconf == c.nt ? CLIP_EMPTY : CLIP_CUT;
@@ -479,14 +491,17 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
   }
   const bool place = res == CLIP_CUT;
   __syncwarp();
-  float lm = 0.f;
-  int base = 0;
-  bool nonfinite = false;
   unsigned vm2[SL];
 #pragma unroll
+  for (int k = 0; k < SL; ++k) vm2[k] = place ? (c.vm[k] & ~m[k]) : c.vm[k];
+  // the nb new vertices into the first free slots; the loop ends once every
+  // group has placed its own
+  int base = 0;
+  bool nonfinite = false;
+#pragma unroll
   for (int k = 0; k < SL; ++k) {
-    const unsigned keep = place ? (c.vm[k] & ~m[k]) : c.vm[k];
-    const unsigned freem = ~keep & group_bits<G>();
+    if (__all_sync(FULL, !place || base >= nb)) break;
+    const unsigned freem = ~vm2[k] & group_bits<G>();
     const int r = base + __popc(freem & ltm);
     const bool recv = place && (freem & lb) && r < nb;
     if (recv) {
@@ -499,15 +514,15 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
       c.vz[k] = x.z;
       c.vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
       nonfinite |= !isfinite(c.vw[k]);
+      lm = fmaxf(lm, c.vw[k]);
     }
-    vm2[k] = keep | group_ballot<G>(recv, gbase);
+    vm2[k] |= group_ballot<G>(recv, gbase);
     base += __popc(freem);
-    if (vm2[k] & lb) lm = fmaxf(lm, c.vw[k]);
   }
   // a new vertex from (nearly) parallel planes: the conflict decisions were
   // inconsistent (a plane through an edge, within rounding); drop the cell
   const bool nf = group_ballot<G>(nonfinite, gbase) != 0u;
-  const float r2 = __uint_as_float(group_max_u<G>(__float_as_uint(lm), gid));
+  const float r2 = group_max_nonneg<G>(lm, gid);
   if (place) {
 #pragma unroll
     for (int k = 0; k < SL; ++k) c.vm[k] = vm2[k];
