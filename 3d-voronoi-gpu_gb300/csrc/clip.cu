@@ -613,15 +613,16 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   }
 }
 
-// Shared state of one lane group of k_build: the site's bisector and
-// start-cube planes, and its clip scratch.
+// Shared state of one lane group of k_build: its clip scratch; the group's
+// planes (4+j bisector j, 4+K+b start-cube face b) are build_plane_stride(K)
+// float4 of the dynamic shared memory, sized by the largest K.
 template <int CAP>
 struct BuildSmem {
-  float4 plane[4 + MAX_SITE_K + BOX_PLANES];  // 4+j bisector j, 4+K+b start-cube face b
   unsigned conf[CAP];
   unsigned bedge[CAP];
   unsigned cnt[WC_N];
 };
+__host__ __device__ constexpr int build_plane_stride(int kmax) { return 4 + kmax + BOX_PLANES; }
 
 // First pass of the exact cell-tet form: WARP / G sites per warp, one per
 // group of G lanes, each group building its site's cell from the bisectors
@@ -638,13 +639,15 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
     unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, int* __restrict__ work, int* __restrict__ out_list,
-    int* __restrict__ out_count) {
+    int* __restrict__ out_count, int kmax) {
   constexpr int NG = WARP / G;
   __shared__ BuildSmem<G * SL> smem_all[CLIP_WARPS * NG];
+  extern __shared__ float4 build_planes[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gid = lane / G, gl = lane % G, gbase = gid * G;
   const unsigned lb = 1u << gl;
   BuildSmem<G * SL>& S = smem_all[wib * NG + gid];
+  float4* const plane = build_planes + (size_t)(wib * NG + gid) * build_plane_stride(kmax);
   for (int i = gl; i < WC_N; i += G) S.cnt[i] = 0u;
   __syncwarp();
 
@@ -665,7 +668,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
         const float4 B = sites[krow[j]];
         const float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
         const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
-        S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
+        plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
       }
     }
     // the start cube centred on the site, containing the domain box
@@ -675,7 +678,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     if (gl < BOX_PLANES) {
       const int ax = gl >> 1;
       const float sgn = (gl & 1) ? -1.f : 1.f;
-      S.plane[4 + K + gl] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
+      plane[4 + K + gl] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
     }
     __syncwarp();
     WarpCell<SL> c;
@@ -699,9 +702,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int pend = 4 + K;
     unsigned seq_cnt = 0u;  // planes (bits 0-7), cuts (8-15), vertex-vs-plane tests (16-31)
     while (__any_sync(FULL, building)) {
-      const float4 P = building ? S.plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
+      const float4 P = building ? plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
       if (building) seq_cnt += 1u + ((unsigned)c.nt << 16);
-      const int r = group_clip<G, SL>(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, gl, gbase, gid, building);
+      const int r = group_clip<G, SL>(c, P, (unsigned)pi, plane, S.conf, S.bedge, gl, gbase, gid, building);
       if (building) {
         if (r == CLIP_EMPTY) {
           state = 1;
@@ -773,7 +776,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     }
     if (__any_sync(FULL, interior)) {
       float vol, mx, my, mz;
-      group_moments<G, SL>(c, S.plane, gl, vol, mx, my, mz);
+      group_moments<G, SL>(c, plane, gl, vol, mx, my, mz);
       if (interior && gl == 0) {
         mom[s] = make_dmom4((double)vol, (double)mx, (double)my, (double)mz);
         S.cnt[WC_INTERIOR]++;
@@ -809,13 +812,13 @@ constexpr int BUILD_G = 8, BUILD_SL = 4;
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
 
 // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
-// fast / redo, cell-tet batched fast / redo, first pass lone / batched
-static int g_clip_resident_blocks[7] = {0, 0, 0, 0, 0, 0, 0};
+// fast / redo, cell-tet batched fast / redo
+static int g_clip_resident_blocks[5] = {0, 0, 0, 0, 0};
 
 template <class F>
-static int resident_blocks(F kernel, int sms, int* out) {
+static int resident_blocks(F kernel, int sms, int* out, size_t dyn_smem = 0) {
   int per_sm = 0;
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, CLIP_WARPS * WARP, 0));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, CLIP_WARPS * WARP, dyn_smem));
   *out = sms * (per_sm > 0 ? per_sm : 1);
   return 0;
 }
@@ -829,11 +832,30 @@ int clip_prepare() {
       resident_blocks(k_clip_site<true, false, SLOTS_FAST>, sms, r + 1) ||
       resident_blocks(k_clip_site<true, false, SLOTS_REDO>, sms, r + 2) ||
       resident_blocks(k_clip_site<true, true, SLOTS_FAST>, sms, r + 3) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_REDO>, sms, r + 4) ||
-      resident_blocks(k_build<false, BUILD_G, BUILD_SL>, sms, r + 5) ||
-      resident_blocks(k_build<true, BUILD_G, BUILD_SL>, sms, r + 6))
+      resident_blocks(k_clip_site<true, true, SLOTS_REDO>, sms, r + 4))
     return -2;
   return 0;
+}
+
+// k_build's dynamic shared memory (its groups' planes) and resident blocks,
+// per largest K (lone / batched)
+static size_t build_dyn_smem(int kmax) {
+  return sizeof(float4) * (size_t)(CLIP_WARPS * (WARP / BUILD_G)) * build_plane_stride(kmax);
+}
+static int g_build_blocks[2][MAX_SITE_K + 1] = {};
+static int build_blocks(bool batched, int kmax) {
+  int& b = g_build_blocks[batched][kmax];
+  if (b == 0) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    const size_t dyn = build_dyn_smem(kmax);
+    if (batched ? resident_blocks(k_build<true, BUILD_G, BUILD_SL>, sms, &b, dyn)
+                : resident_blocks(k_build<false, BUILD_G, BUILD_SL>, sms, &b, dyn))
+      return 0;
+  }
+  return b;
 }
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
@@ -841,7 +863,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters,
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                     cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
@@ -878,12 +900,19 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
         out_count, work);
   };
   if (exact) {
+    if (kmax < 1 || kmax > MAX_SITE_K) {
+      set_error("clip: largest K %d outside [1, %d]", kmax, MAX_SITE_K);
+      return -1;
+    }
+    const int bb = build_blocks(probs != nullptr, kmax);
+    if (bb <= 0) return -2;
+    const size_t dyn = build_dyn_smem(kmax);
     if (probs)
-      k_build<true, BUILD_G, BUILD_SL><<<g_clip_resident_blocks[6], CLIP_WARPS * WARP, 0, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0);
+      k_build<true, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax);
     else
-      k_build<false, BUILD_G, BUILD_SL><<<g_clip_resident_blocks[5], CLIP_WARPS * WARP, 0, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0);
+      k_build<false, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax);
   }
   const int* in_list = exact ? rest : nullptr;
   const int* in_count = exact ? counters + 0 : nullptr;

@@ -215,7 +215,7 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
-                        e->reach_max, nullptr, e->redo_list, e->redo_count, st))
+                        e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,

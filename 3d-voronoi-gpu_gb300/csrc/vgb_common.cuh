@@ -207,14 +207,15 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
-                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters,
+                    const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                     cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.  lists (2n ints) and counters (at least 5
 // ints): cell-tet scratch for the sites one pass hands to the next (the
 // lane-group first pass of the exact form, the one-warp pass, the 128-vertex
 // pass) and the passes' work counters.  The engine and the batch keep a
-// sixth int after them for the kNN's work counter.
+// sixth int after them for the kNN's work counter.  kmax: the largest K of
+// the problems (it sizes the first pass's shared memory).
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.
