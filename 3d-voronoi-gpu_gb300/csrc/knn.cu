@@ -98,6 +98,22 @@ __device__ __forceinline__ void shell_cell(int w, int t, int& di, int& dj, int& 
   }
 }
 
+// Shells 0 .. KNN_TAB_W come from a table built once per block: entry
+// (2w-1)^3 + t holds the offset of the t-th cell of shell w, a byte per axis
+// biased by 8 (shell_cell costs a few integer divisions per cell).
+constexpr int KNN_TAB_W = 4;
+constexpr int KNN_TAB = (2 * KNN_TAB_W + 1) * (2 * KNN_TAB_W + 1) * (2 * KNN_TAB_W + 1);
+
+__device__ __forceinline__ void shell_table(unsigned* tab) {
+  for (int i = threadIdx.x; i < KNN_TAB; i += blockDim.x) {
+    int w = 0;
+    while ((2 * w + 1) * (2 * w + 1) * (2 * w + 1) <= i) ++w;
+    int di = 0, dj = 0, dk = 0;
+    if (w > 0) shell_cell(w, i - (2 * w - 1) * (2 * w - 1) * (2 * w - 1), di, dj, dk);
+    tab[i] = (unsigned)(di + 8) | ((unsigned)(dj + 8) << 8) | ((unsigned)(dk + 8) << 16);
+  }
+}
+
 // Ascending bitonic sort of one key per lane.
 __device__ __forceinline__ u64 warp_sort32(u64 x, int lane) {
 #pragma unroll
@@ -164,6 +180,9 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
+  __shared__ unsigned shell_tab[KNN_TAB];
+  shell_table(shell_tab);
+  __syncthreads();
   // with a work counter, warps draw the next query from it (one wave of
   // resident blocks: a warp that drew cheap queries takes more); without,
   // queries are dealt round-robin
@@ -223,7 +242,14 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
         const int t = cb + lane;
         if (t < ncell) {
           int di = 0, dj = 0, dk = 0;
-          if (w > 0) shell_cell(w, t, di, dj, dk);
+          if (w > KNN_TAB_W) {
+            shell_cell(w, t, di, dj, dk);
+          } else if (w > 0) {
+            const unsigned u = shell_tab[(2 * w - 1) * (2 * w - 1) * (2 * w - 1) + t];
+            di = (int)(u & 0xffu) - 8;
+            dj = (int)((u >> 8) & 0xffu) - 8;
+            dk = (int)(u >> 16) - 8;
+          }
           const int i = ci + di, j = cj + dj, k = ck + dk;
           if (i >= 0 && i < dim && j >= 0 && j < dim && k >= 0 && k < dim &&
               (tau == KEY_NONE || box_d2(Q, i, j, k, dim, h) <= __uint_as_float((unsigned)(tau >> 32)))) {
