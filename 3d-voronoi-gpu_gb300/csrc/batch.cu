@@ -70,6 +70,7 @@ struct vgb_batch {
   unsigned* secmiss = nullptr;
   int* redo_list = nullptr;
   int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
+  vgb::CellStore store{};          // cells the first clip pass built and handed on (by site)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t tev[2] = {};
 };
@@ -100,7 +101,7 @@ void free_batch(vgb_batch* b) {
   void* bufs[] = {b->d_probs, b->site_prob, b->tet_prob, b->verts, b->tets, b->sites, b->sites_tmp,
                   b->cell_start, b->cell_fill, b->site_cell, b->scan_tmp, b->pos_of_id, b->tet_order,
                   b->tet_cell_start, b->tcell, b->knn, b->mom, b->stats, b->field, b->field_sat, b->reach,
-                  b->tet_sph, b->reach_max, b->secmiss, b->redo_list, b->redo_count};
+                  b->tet_sph, b->reach_max, b->secmiss, b->redo_list, b->redo_count, b->store.tri, b->store.nt};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->st) cudaStreamDestroy(b->st);
@@ -168,7 +169,7 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   if (clip_site_major(true, b->sites, b->n, b->knn, b->d_probs, b->site_prob, none, b->verts, b->tets, nullptr,
                       nullptr, b->mom, b->stats, b->field, b->field_sat, b->tet_order, b->tet_cell_start, b->tet_sph,
                       b->reach, b->reach_max, count_secmiss ? b->secmiss : nullptr, b->redo_list, b->redo_count,
-                      b->kmax, st))
+                      b->kmax, b->store, st))
     return VGB_ERR_CUDA;
   if (finish_sites(b->sites, b->n, b->mom, update, st)) return VGB_ERR_CUDA;
   return VGB_OK;
@@ -342,7 +343,8 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       (rc = balloc(&b->stats, VGB_STAT_COUNT)) || (rc = balloc(&b->field, f_off)) ||
       (rc = balloc(&b->field_sat, q_off)) || (rc = balloc(&b->reach, b->n_tet)) ||
       (rc = balloc(&b->tet_sph, b->n_tet)) || (rc = balloc(&b->reach_max, n_prob)) ||
-      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 2 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 8))) {
+      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 2 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 8)) ||
+      (rc = balloc(&b->store.tri, (size_t)b->n * vgb::STORE_VERTS)) || (rc = balloc(&b->store.nt, b->n))) {
     free_batch(b);
     return rc;
   }

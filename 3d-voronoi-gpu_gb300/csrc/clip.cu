@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
     const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss,
     const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ out_list,
-    int* __restrict__ out_count, int* __restrict__ work) {
+    int* __restrict__ out_count, int* __restrict__ work, const CellStore store) {
   __shared__ SiteSmem<SL> smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -175,6 +175,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
   for (int it = work ? next_item(0) : blockIdx.x * CLIP_WARPS + wib; it < n_items; it = next_item(it)) {
     const int s = in_list ? in_list[it] : it;
     bool abandon = false;
+    // the cell the first pass built, when it stored one
+    const int stored = (CELL_TET && store.nt) ? store.nt[s] : 0;
     // the site's problem; its descriptor fields are read where used (from
     // global memory or the kernel parameters) rather than held in registers
     const int pidx = BATCHED ? site_prob[s] : 0;
@@ -236,7 +238,29 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       // for the box bound, or the next surviving candidate
       WarpCell<SL> c;
       cell_clear(c);
-      if (job == 0) {
+      if (job == 0 && stored) {
+        // its vertices from its plane triples, the evaluation that made them
+        const int nt0 = stored & 255;
+        float lm = 0.f;
+#pragma unroll
+        for (int k = 0; k < SL; ++k) {
+          const int left = nt0 - k * WARP;
+          c.vm[k] = left >= WARP ? FULL : left > 0 ? (1u << left) - 1u : 0u;
+          const int j = k * WARP + lane;
+          if (j < nt0) {
+            const unsigned T = store.tri[(size_t)s * STORE_VERTS + j];
+            const float3 x = vertex_of(S.plane[tri_at(T, 0)], S.plane[tri_at(T, 1)], S.plane[tri_at(T, 2)]);
+            c.tri[k] = T;
+            c.vx[k] = x.x;
+            c.vy[k] = x.y;
+            c.vz[k] = x.z;
+            c.vw[k] = norm2_rn(x);
+            lm = fmaxf(lm, c.vw[k]);
+          }
+        }
+        c.nt = nt0;
+        c.r2 = warp_max_nonneg(lm);
+      } else if (job == 0) {
         const float L = cube_half();
         if (lane < 8) {
           // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
@@ -291,8 +315,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
             // beyond
             const float4 sp = tet_sph[idx];
             const float ex = sp.x - seed.x, ey = sp.y - seed.y, ez = sp.z - seed.z;
-            const float dm = sqrtf(ex * ex + ey * ey + ez * ez);
-            alive = dm <= (Rc + sp.w) * 1.0001f + 1e-3f && dm <= reach[idx] * 1.0001f + 1e-2f;
+            const float dm = sqrtf(dot3_rn(ex, ey, ez, ex, ey, ez));
+            alive = dm <= __fmaf_rn(Rc + sp.w, 1.0001f, 1e-3f) && dm <= __fmaf_rn(reach[idx], 1.0001f, 1e-2f);
           }
           if (alive) {
             t = exact ? tet_order[idx] : site_tets[idx];
@@ -308,12 +332,10 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
               // bounding spheres: the cell lies within Rc of the site
               const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
                           mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
-              float rt2 = (v0.x - mx) * (v0.x - mx) + (v0.y - my) * (v0.y - my) + (v0.z - mz) * (v0.z - mz);
-              rt2 = fmaxf(rt2, (v1.x - mx) * (v1.x - mx) + (v1.y - my) * (v1.y - my) + (v1.z - mz) * (v1.z - mz));
-              rt2 = fmaxf(rt2, (v2.x - mx) * (v2.x - mx) + (v2.y - my) * (v2.y - my) + (v2.z - mz) * (v2.z - mz));
-              rt2 = fmaxf(rt2, (v3.x - mx) * (v3.x - mx) + (v3.y - my) * (v3.y - my) + (v3.z - mz) * (v3.z - mz));
-              const float dm = sqrtf(mx * mx + my * my + mz * mz);
-              if (dm > (Rc + sqrtf(rt2)) * 1.0001f + 1e-3f) alive = false;
+              auto d2 = [&](float3 v) { return dot3_rn(v.x - mx, v.y - my, v.z - mz, v.x - mx, v.y - my, v.z - mz); };
+              const float rt2 = fmaxf(fmaxf(d2(v0), d2(v1)), fmaxf(d2(v2), d2(v3)));
+              const float dm = sqrtf(dot3_rn(mx, my, mz, mx, my, mz));
+              if (dm > __fmaf_rn(Rc + sqrtf(rt2), 1.0001f, 1e-3f)) alive = false;
             }
             // a tet whose four corners are strictly outside one face of the
             // cell cannot meet it
@@ -414,9 +436,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       // domain-box faces, or the tet's four faces
       const bool bis = job == 0 || !CELL_TET;
       const int pbeg = job == 1 ? 4 + K + BOX_PLANES : bis ? 4 : 0;
-      const int pend = job == 1 ? pbeg + BOX_PLANES : bis ? 4 + K : 4;
+      const int pend = job == 1 ? pbeg + BOX_PLANES : (job == 0 && stored) ? pbeg : bis ? 4 + K : 4;
       int state = 0;  // 0 kept, 1 empty, 2 dropped
-      bool secmiss = bis;
+      bool secmiss = (job == 0 && stored) ? (stored >> 8) != 0 : bis;
       // counters of the sequence, packed: planes (bits 0-7), cuts (8-15),
       // vertex-vs-plane tests (16-31); at most 144 planes of 96 vertices
       unsigned seq_cnt = 0u;
@@ -493,7 +515,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         // left it as built).  First the ball of radius Rc against the site
         // cell's clear radius (one byte), then the cell's vertex bounding box
         // against the summed table.
-        const float Rq = Rc * 1.001f + 0.01f;
+        const float Rq = __fmaf_rn(Rc, 1.001f, 0.01f);
         const int fdim = field ? PD(fdim) : 1;
         const int fv = field && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
                                seed.y <= 1000.f && seed.z >= 0.f && seed.z <= 1000.f
@@ -513,7 +535,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           if (!interior) {
             float lo[3], hi[3];
             cell_bounds(c, lane, lo, hi);
-            const float m = 1e-3f * Rc + 0.01f;
+            const float m = __fmaf_rn(1e-3f, Rc, 0.01f);
             const float x0 = seed.x + lo[0] - m, x1 = seed.x + hi[0] + m, y0 = seed.y + lo[1] - m,
                         y1 = seed.y + hi[1] + m, z0 = seed.z + lo[2] - m, z1 = seed.z + hi[2] + m;
             if (x0 >= 0.f && x1 <= 1000.f && y0 >= 0.f && y1 <= 1000.f && z0 >= 0.f && z1 <= 1000.f) {
@@ -558,7 +580,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           // farther than the largest reach
           if (exact) {
             const int dim = PD(dim);
-            const float R = fminf(Rc + PD(rt_max) * 1.001f, __uint_as_float(reach_max_bits[pidx])) + 0.01f;
+            const float R = fminf(__fmaf_rn(PD(rt_max), 1.001f, Rc), __uint_as_float(reach_max_bits[pidx])) + 0.01f;
             i0 = grid_axis(seed.x - R, dim);
             i1 = grid_axis(seed.x + R, dim);
             j0 = grid_axis(seed.y - R, dim);
@@ -639,7 +661,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
     unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, int* __restrict__ work, int* __restrict__ out_list,
-    int* __restrict__ out_count, int kmax) {
+    int* __restrict__ out_count, int kmax, const CellStore store) {
   constexpr int NG = WARP / G;
   __shared__ BuildSmem<G * SL> smem_all[CLIP_WARPS * NG];
   extern __shared__ float4 build_planes[];
@@ -730,7 +752,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     // test of k_clip_site)
     const bool built = has && state == 0 && !secmiss;
     const float Rc = sqrtf(c.r2);
-    const float Rq = Rc * 1.001f + 0.01f;
+    const float Rq = __fmaf_rn(Rc, 1.001f, 0.01f);
     const int fdim = field ? PD(fdim) : 1;
     const int fv = built && field && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f && seed.y <= 1000.f &&
                            seed.z >= 0.f && seed.z <= 1000.f
@@ -759,7 +781,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
                   lo2 = ord_val(group_min_u<G>(ord_key(l2), gid));
       const float hi0 = ord_val(group_max_u<G>(ord_key(h0), gid)), hi1 = ord_val(group_max_u<G>(ord_key(h1), gid)),
                   hi2 = ord_val(group_max_u<G>(ord_key(h2), gid));
-      const float m = 1e-3f * Rc + 0.01f;
+      const float m = __fmaf_rn(1e-3f, Rc, 0.01f);
       const float x0 = seed.x + lo0 - m, x1 = seed.x + hi0 + m, y0 = seed.y + lo1 - m, y1 = seed.y + hi1 + m,
                   z0 = seed.z + lo2 - m, z1 = seed.z + hi2 + m;
       if (need_box && x0 >= 0.f && x1 <= 1000.f && y0 >= 0.f && y1 <= 1000.f && z0 >= 0.f && z1 <= 1000.f) {
@@ -783,11 +805,24 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
         S.cnt[WC_FINAL] += (unsigned)c.nt;
       }
     }
+    // a cell handed on is stored (when it was built) for the one-warp pass
+    const bool keep = has && !interior && state == 0;
+    if (store.tri) {
+      int base = 0;
+#pragma unroll
+      for (int k = 0; k < SL; ++k) {
+        if (keep && (c.vm[k] & lb)) store.tri[(size_t)s * STORE_VERTS + base + __popc(c.vm[k] & (lb - 1u))] = c.tri[k];
+        base += __popc(c.vm[k]);
+      }
+    }
     if (has && gl == 0) {
       S.cnt[WC_PLANES] += seq_cnt & 0xffu;
       S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
       S.cnt[WC_CONFLICT] += seq_cnt >> 16;
-      if (!interior) out_list[atomicAdd(out_count, 1)] = s;
+      if (!interior) {
+        if (store.nt) store.nt[s] = keep ? (c.nt | (secmiss ? 256 : 0)) : 0;
+        out_list[atomicAdd(out_count, 1)] = s;
+      }
     }
     __syncwarp();
 #undef PD
@@ -809,6 +844,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
 // reference cell-tet form starts at the one-warp pass.  The tet-cell method
 // runs with 3 (96, the reference's capacity).
 constexpr int BUILD_G = 8, BUILD_SL = 4;
+static_assert(BUILD_G * BUILD_SL <= STORE_VERTS, "a stored cell holds a first-pass cell");
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
 
 // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
@@ -864,7 +900,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
-                    cudaStream_t st) {
+                    const CellStore& store, cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
   if (!cell_tet && probs) {
@@ -880,7 +916,8 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     const long long want = (long long)g_clip_resident_blocks[0] * 4, need = (n + CLIP_WARPS - 1) / CLIP_WARPS;
     k_clip_site<false, false, SLOTS_TET_CELL><<<(int)(want < need ? want : need), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
-        nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr);
+        nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr,
+        CellStore{});
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
@@ -892,12 +929,14 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
   int* const rest = lists + n;
   VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 5 * sizeof(int), st));
   // every pass: one wave of resident blocks whose warps draw sites from a counter
+  // the first pass's stored cells (exact form only)
+  const CellStore cs = exact ? store : CellStore{};
   auto launch = [&](auto kernel, int variant, const int* in_list, const int* in_count, int* out_list, int* out_count,
                     int* work) {
     kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
         tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, in_list, in_count, out_list,
-        out_count, work);
+        out_count, work, cs);
   };
   if (exact) {
     if (kmax < 1 || kmax > MAX_SITE_K) {
@@ -909,10 +948,12 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     const size_t dyn = build_dyn_smem(kmax);
     if (probs)
       k_build<true, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax);
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
+          cs);
     else
       k_build<false, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax);
+          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
+          cs);
   }
   const int* in_list = exact ? rest : nullptr;
   const int* in_count = exact ? counters + 0 : nullptr;

@@ -37,25 +37,39 @@ __device__ __forceinline__ float plane_eval(float4 P, float x, float y, float z)
 }
 
 // Vertex of three planes n_i.x + w_i = 0 (Cramer's rule, as a cross-product
-// combination).
-__device__ __forceinline__ float3 vertex_of(float4 a, float4 b, float4 c) {
-  float3 bc = make_float3(b.y * c.z - b.z * c.y, b.z * c.x - b.x * c.z, b.x * c.y - b.y * c.x);
-  float3 ca = make_float3(c.y * a.z - c.z * a.y, c.z * a.x - c.x * a.z, c.x * a.y - c.y * a.x);
-  float3 ab = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-  float det = a.x * bc.x + a.y * bc.y + a.z * bc.z;
-  float s = __fdividef(-1.f, det);
-  return make_float3(s * (a.w * bc.x + b.w * ca.x + c.w * ab.x), s * (a.w * bc.y + b.w * ca.y + c.w * ab.y),
-                     s * (a.w * bc.z + b.w * ca.z + c.w * ab.z));
+// combination).  Every product and sum is an explicit rounding intrinsic, so
+// each inlined copy (the clips, and the passes that recompute a stored
+// cell's vertices from its plane triples) gives the same bits.
+__device__ __forceinline__ float cross_term(float p, float q, float r, float t) {
+  return __fmaf_rn(p, q, -__fmul_rn(r, t));  // p q - r t
 }
+__device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, float b0, float b1, float b2) {
+  return __fmaf_rn(a0, b0, __fmaf_rn(a1, b1, __fmul_rn(a2, b2)));
+}
+__device__ __forceinline__ float3 vertex_of(float4 a, float4 b, float4 c) {
+  const float3 bc = make_float3(cross_term(b.y, c.z, b.z, c.y), cross_term(b.z, c.x, b.x, c.z),
+                                cross_term(b.x, c.y, b.y, c.x));
+  const float3 ca = make_float3(cross_term(c.y, a.z, c.z, a.y), cross_term(c.z, a.x, c.x, a.z),
+                                cross_term(c.x, a.y, c.y, a.x));
+  const float3 ab = make_float3(cross_term(a.y, b.z, a.z, b.y), cross_term(a.z, b.x, a.x, b.z),
+                                cross_term(a.x, b.y, a.y, b.x));
+  const float det = dot3_rn(a.x, a.y, a.z, bc.x, bc.y, bc.z);
+  const float s = __fdividef(-1.f, det);
+  return make_float3(__fmul_rn(s, dot3_rn(a.w, b.w, c.w, bc.x, ca.x, ab.x)),
+                     __fmul_rn(s, dot3_rn(a.w, b.w, c.w, bc.y, ca.y, ab.y)),
+                     __fmul_rn(s, dot3_rn(a.w, b.w, c.w, bc.z, ca.z, ab.z)));
+}
+// |x|^2, with the same rounding everywhere
+__device__ __forceinline__ float norm2_rn(float3 x) { return dot3_rn(x.x, x.y, x.z, x.x, x.y, x.z); }
 
 // Plane through three points, normal (p1-p0)x(p2-p0): positive inside a
 // positively oriented tet for the faces (c,b,d), (a,c,d), (b,a,d), (a,b,c)
 // (voronoi.cu:119-123, 179).
 __device__ __forceinline__ float4 face_plane(float3 p0, float3 p1, float3 p2) {
-  float ux = p1.x - p0.x, uy = p1.y - p0.y, uz = p1.z - p0.z;
-  float vx = p2.x - p0.x, vy = p2.y - p0.y, vz = p2.z - p0.z;
-  float nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-  return make_float4(nx, ny, nz, -(nx * p0.x + ny * p0.y + nz * p0.z));
+  const float ux = p1.x - p0.x, uy = p1.y - p0.y, uz = p1.z - p0.z;
+  const float vx = p2.x - p0.x, vy = p2.y - p0.y, vz = p2.z - p0.z;
+  const float nx = cross_term(uy, vz, uz, vy), ny = cross_term(uz, vx, ux, vz), nz = cross_term(ux, vy, uy, vx);
+  return make_float4(nx, ny, nz, -dot3_rn(nx, ny, nz, p0.x, p0.y, p0.z));
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -245,7 +259,7 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
       c.vx[k] = x.x;
       c.vy[k] = x.y;
       c.vz[k] = x.z;
-      c.vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
+      c.vw[k] = norm2_rn(x);
       nonfinite |= !isfinite(c.vw[k]);
     }
     c.vm[k] = keep | __ballot_sync(FULL, recv);
@@ -271,30 +285,32 @@ __device__ __forceinline__ void vertex_moments(float3 A, float4 p0, float4 p1, f
   float3 P[6];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    float4 n = pl[i];
-    float nn = n.x * n.x + n.y * n.y + n.z * n.z;
-    float lam = nn > 0.f ? __fdividef(-n.w, nn) : 0.f;
-    P[2 * i] = make_float3(lam * n.x, lam * n.y, lam * n.z);
+    const float4 n = pl[i];
+    const float nn = dot3_rn(n.x, n.y, n.z, n.x, n.y, n.z);
+    const float lam = nn > 0.f ? __fdividef(-n.w, nn) : 0.f;
+    P[2 * i] = make_float3(__fmul_rn(lam, n.x), __fmul_rn(lam, n.y), __fmul_rn(lam, n.z));
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    float4 a = pl[i], b = pl[(i + 1) % 3];
-    float dx = a.y * b.z - a.z * b.y, dy = a.z * b.x - a.x * b.z, dz = a.x * b.y - a.y * b.x;
-    float dd = dx * dx + dy * dy + dz * dz;
-    float t = dd > 0.f ? __fdividef(A.x * dx + A.y * dy + A.z * dz, dd) : 0.f;
-    P[2 * i + 1] = make_float3(A.x - t * dx, A.y - t * dy, A.z - t * dz);
+    const float4 a = pl[i], b = pl[(i + 1) % 3];
+    const float dx = cross_term(a.y, b.z, a.z, b.y), dy = cross_term(a.z, b.x, a.x, b.z),
+                dz = cross_term(a.x, b.y, a.y, b.x);
+    const float dd = dot3_rn(dx, dy, dz, dx, dy, dz);
+    const float t = dd > 0.f ? __fdividef(dot3_rn(A.x, A.y, A.z, dx, dy, dz), dd) : 0.f;
+    P[2 * i + 1] = make_float3(__fmaf_rn(-t, dx, A.x), __fmaf_rn(-t, dy, A.y), __fmaf_rn(-t, dz, A.z));
   }
   v6 = 0.f;
   m24 = make_float3(0.f, 0.f, 0.f);
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
-    float3 a = P[m], b = P[(m + 1) % 6];
-    float cx = a.y * b.z - a.z * b.y, cy = a.z * b.x - a.x * b.z, cz = a.x * b.y - a.y * b.x;
-    float d = A.x * cx + A.y * cy + A.z * cz;  // det3(a, b, A)
-    v6 += d;
-    m24.x += d * (a.x + b.x + A.x);
-    m24.y += d * (a.y + b.y + A.y);
-    m24.z += d * (a.z + b.z + A.z);
+    const float3 a = P[m], b = P[(m + 1) % 6];
+    const float cx = cross_term(a.y, b.z, a.z, b.y), cy = cross_term(a.z, b.x, a.x, b.z),
+                cz = cross_term(a.x, b.y, a.y, b.x);
+    const float d = dot3_rn(A.x, A.y, A.z, cx, cy, cz);  // det3(a, b, A)
+    v6 = __fadd_rn(v6, d);
+    m24.x = __fmaf_rn(d, __fadd_rn(__fadd_rn(a.x, b.x), A.x), m24.x);
+    m24.y = __fmaf_rn(d, __fadd_rn(__fadd_rn(a.y, b.y), A.y), m24.y);
+    m24.z = __fmaf_rn(d, __fadd_rn(__fadd_rn(a.z, b.z), A.z), m24.z);
   }
 }
 
@@ -311,16 +327,16 @@ __device__ __forceinline__ void warp_moments(const WarpCell<SL>& c, const float4
   for (int k = 0; k < SL; ++k)
     if (c.vm[k] & lane_bit) { sx += c.vx[k]; sy += c.vy[k]; sz += c.vz[k]; }
   const float inv = __frcp_rn((float)c.nt);
-  const float cx = warp_sum(sx) * inv, cy = warp_sum(sy) * inv, cz = warp_sum(sz) * inv;
+  const float cx = __fmul_rn(warp_sum(sx), inv), cy = __fmul_rn(warp_sum(sy), inv), cz = __fmul_rn(warp_sum(sz), inv);
   float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
 #pragma unroll
   for (int k = 0; k < SL; ++k) {
     if (c.vm[k] & lane_bit) {
       const unsigned T = c.tri[k];
       float4 q0 = planes[tri_at(T, 0)], q1 = planes[tri_at(T, 1)], q2 = planes[tri_at(T, 2)];
-      q0.w += q0.x * cx + q0.y * cy + q0.z * cz;  // planes relative to the apex
-      q1.w += q1.x * cx + q1.y * cy + q1.z * cz;
-      q2.w += q2.x * cx + q2.y * cy + q2.z * cz;
+      q0.w = __fadd_rn(q0.w, dot3_rn(q0.x, q0.y, q0.z, cx, cy, cz));  // planes relative to the apex
+      q1.w = __fadd_rn(q1.w, dot3_rn(q1.x, q1.y, q1.z, cx, cy, cz));
+      q2.w = __fadd_rn(q2.w, dot3_rn(q2.x, q2.y, q2.z, cx, cy, cz));
       float v6;
       float3 m24;
       vertex_moments(make_float3(c.vx[k] - cx, c.vy[k] - cy, c.vz[k] - cz), q0, q1, q2, v6, m24);
@@ -330,10 +346,10 @@ __device__ __forceinline__ void warp_moments(const WarpCell<SL>& c, const float4
       lmz += m24.z;
     }
   }
-  vol = warp_sum(lv) * (1.f / 6.f);
-  mx = fmaf(warp_sum(lmx), 1.f / 24.f, vol * cx);
-  my = fmaf(warp_sum(lmy), 1.f / 24.f, vol * cy);
-  mz = fmaf(warp_sum(lmz), 1.f / 24.f, vol * cz);
+  vol = __fmul_rn(warp_sum(lv), 1.f / 6.f);
+  mx = __fmaf_rn(warp_sum(lmx), 1.f / 24.f, __fmul_rn(vol, cx));
+  my = __fmaf_rn(warp_sum(lmy), 1.f / 24.f, __fmul_rn(vol, cy));
+  mz = __fmaf_rn(warp_sum(lmz), 1.f / 24.f, __fmul_rn(vol, cz));
 }
 
 // ---------------------------------------------------------------------------
@@ -512,7 +528,7 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
       c.vx[k] = x.x;
       c.vy[k] = x.y;
       c.vz[k] = x.z;
-      c.vw[k] = x.x * x.x + x.y * x.y + x.z * x.z;
+      c.vw[k] = norm2_rn(x);
       nonfinite |= !isfinite(c.vw[k]);
       lm = fmaxf(lm, c.vw[k]);
     }
@@ -545,16 +561,17 @@ __device__ __forceinline__ void group_moments(const WarpCell<SL>& c, const float
   for (int k = 0; k < SL; ++k)
     if (c.vm[k] & lb) { sx += c.vx[k]; sy += c.vy[k]; sz += c.vz[k]; }
   const float inv = __frcp_rn((float)max(c.nt, 1));
-  const float cx = group_sum<G>(sx) * inv, cy = group_sum<G>(sy) * inv, cz = group_sum<G>(sz) * inv;
+  const float cx = __fmul_rn(group_sum<G>(sx), inv), cy = __fmul_rn(group_sum<G>(sy), inv),
+              cz = __fmul_rn(group_sum<G>(sz), inv);
   float lv = 0.f, lmx = 0.f, lmy = 0.f, lmz = 0.f;
 #pragma unroll
   for (int k = 0; k < SL; ++k) {
     if (c.vm[k] & lb) {
       const unsigned T = c.tri[k];
       float4 q0 = planes[tri_at(T, 0)], q1 = planes[tri_at(T, 1)], q2 = planes[tri_at(T, 2)];
-      q0.w += q0.x * cx + q0.y * cy + q0.z * cz;  // planes relative to the apex
-      q1.w += q1.x * cx + q1.y * cy + q1.z * cz;
-      q2.w += q2.x * cx + q2.y * cy + q2.z * cz;
+      q0.w = __fadd_rn(q0.w, dot3_rn(q0.x, q0.y, q0.z, cx, cy, cz));  // planes relative to the apex
+      q1.w = __fadd_rn(q1.w, dot3_rn(q1.x, q1.y, q1.z, cx, cy, cz));
+      q2.w = __fadd_rn(q2.w, dot3_rn(q2.x, q2.y, q2.z, cx, cy, cz));
       float v6;
       float3 m24;
       vertex_moments(make_float3(c.vx[k] - cx, c.vy[k] - cy, c.vz[k] - cz), q0, q1, q2, v6, m24);
@@ -564,10 +581,10 @@ __device__ __forceinline__ void group_moments(const WarpCell<SL>& c, const float
       lmz += m24.z;
     }
   }
-  vol = group_sum<G>(lv) * (1.f / 6.f);
-  mx = fmaf(group_sum<G>(lmx), 1.f / 24.f, vol * cx);
-  my = fmaf(group_sum<G>(lmy), 1.f / 24.f, vol * cy);
-  mz = fmaf(group_sum<G>(lmz), 1.f / 24.f, vol * cz);
+  vol = __fmul_rn(group_sum<G>(lv), 1.f / 6.f);
+  mx = __fmaf_rn(group_sum<G>(lmx), 1.f / 24.f, __fmul_rn(vol, cx));
+  my = __fmaf_rn(group_sum<G>(lmy), 1.f / 24.f, __fmul_rn(vol, cy));
+  mz = __fmaf_rn(group_sum<G>(lmz), 1.f / 24.f, __fmul_rn(vol, cz));
 }
 
 }  // namespace vgb

@@ -60,6 +60,7 @@ struct vgb_engine {
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
   int* redo_list = nullptr;        // cell-tet: sites handed from one clip pass to the next (2n)
   int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
+  vgb::CellStore store{};          // exact form: cells the first clip pass built and handed on (by site)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -173,7 +174,7 @@ void free_engine(vgb_engine* e) {
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
                   e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph,
-                  e->redo_list, e->redo_count};
+                  e->redo_list, e->redo_count, e->store.tri, e->store.nt};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -215,7 +216,7 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
-                        e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, st))
+                        e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, e->store, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -358,7 +359,9 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
       (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 2 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 8)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
-      (rc = dalloc(&e->stats, VGB_STAT_COUNT))) {
+      (rc = dalloc(&e->stats, VGB_STAT_COUNT)) ||
+      (rc = dalloc(&e->store.tri, exact_form ? (size_t)n_site * STORE_VERTS : 1)) ||
+      (rc = dalloc(&e->store.nt, exact_form ? (size_t)n_site : 1))) {
     free_engine(e);
     return rc;
   }

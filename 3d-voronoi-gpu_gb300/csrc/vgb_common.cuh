@@ -202,13 +202,24 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 // taken whole, other cells are clipped by every tet within reach (tets sorted
 // by centroid cell of the site grid, dim^3 cells).  Otherwise the candidate
 // lists site_start / site_tets are used.
+// Cells the first pass of the exact form built but handed on, by site: at
+// most STORE_VERTS plane-id triples, packed, and their count | (security
+// radius missed) << 8, 0 for none.  The one-warp pass starts from the
+// stored cell (its vertices recomputed from the triples) instead of
+// building it again.
+constexpr int STORE_VERTS = 32;
+struct CellStore {
+  unsigned* tri;  // [n][STORE_VERTS]
+  int* nt;        // [n]
+};
+
 int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
                     const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
-                    cudaStream_t st);
+                    const CellStore& store, cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.  lists (2n ints) and counters (at least 5
 // ints): cell-tet scratch for the sites one pass hands to the next (the
