@@ -388,7 +388,11 @@ def run_ours(args):
     clip_flops = (FLOPS_CONFLICT * stats["conflict_tests"] + FLOPS_CULL * stats["cull_tests"] +
                   FLOPS_NEW_VERTEX * stats["new_vertices"] + FLOPS_FINAL_VERTEX * stats["final_vertices"])
     clip_tf = clip_flops / (phases["clip"] / 1e3) / 1e12
-    kname = {"cell_tet": "k_clip_site<true>", "site_major": "k_clip_site<false>", "plain": "k_clip_plain"}[args.method]
+    # the clip phase: the exact form runs the lane-group first pass (k_build),
+    # the one-warp pass over the sites it hands on and the 128-vertex pass
+    kname = ("k_build + k_clip_site<cell_tet> x2 (clip phase)" if exact else
+             {"cell_tet": "k_clip_site<cell_tet> x2 (clip phase)", "site_major": "k_clip_site<tet_cell>",
+              "plain": "k_clip_plain"}[args.method])
     ktraffic = profile_traffic("clip_exact" if exact else {"cell_tet": "clip_cell_tet", "site_major": "clip_tet_cell",
                                                           "plain": "clip_plain"}[args.method], args.workload)
     roofline = {"kernel": kname,
