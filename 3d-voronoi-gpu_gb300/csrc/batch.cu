@@ -69,7 +69,7 @@ struct vgb_batch {
   unsigned* reach_max = nullptr;
   unsigned* secmiss = nullptr;
   int* redo_list = nullptr;
-  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
+  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counters (12)
   vgb::CellStore store{};          // cells the first clip pass built and handed on (by site)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t tev[2] = {};
@@ -158,8 +158,10 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
                 st))
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(b->sites, b->sites_tmp, sizeof(float4) * b->n, cudaMemcpyDeviceToDevice, st));
+  // KNN_TIER neighbours first; the rest for the sites that need them (clip phase)
+  const int tier = b->kmax > KNN_TIER ? KNN_TIER : 0;
   if (knn_sites(b->sites, b->n, b->cell_start, b->d_probs, b->site_prob, none, b->kmax, b->pos_of_id, b->knn,
-                b->redo_count + 5, st))
+                b->redo_count + 5, st, tier))
     return VGB_ERR_CUDA;
   if (tet_reach(b->sites, b->cell_start, b->d_probs, b->tet_prob, none, b->n_prob, b->tet_sph, b->n_tet, b->reach,
                 b->reach_max, st))
@@ -169,7 +171,7 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   if (clip_site_major(true, b->sites, b->n, b->knn, b->d_probs, b->site_prob, none, b->verts, b->tets, nullptr,
                       nullptr, b->mom, b->stats, b->field, b->field_sat, b->tet_order, b->tet_cell_start, b->tet_sph,
                       b->reach, b->reach_max, count_secmiss ? b->secmiss : nullptr, b->redo_list, b->redo_count,
-                      b->kmax, b->store, st))
+                      b->kmax, b->store, tier, b->cell_start, b->pos_of_id, st))
     return VGB_ERR_CUDA;
   if (finish_sites(b->sites, b->n, b->mom, update, st)) return VGB_ERR_CUDA;
   return VGB_OK;
@@ -343,10 +345,17 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       (rc = balloc(&b->stats, VGB_STAT_COUNT)) || (rc = balloc(&b->field, f_off)) ||
       (rc = balloc(&b->field_sat, q_off)) || (rc = balloc(&b->reach, b->n_tet)) ||
       (rc = balloc(&b->tet_sph, b->n_tet)) || (rc = balloc(&b->reach_max, n_prob)) ||
-      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 2 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 8)) ||
+      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 3 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 12)) ||
       (rc = balloc(&b->store.tri, (size_t)b->n * vgb::STORE_VERTS)) || (rc = balloc(&b->store.nt, b->n))) {
     free_batch(b);
     return rc;
+  }
+  // neighbour rows start as valid indices (with the kNN in tiers a row's tail
+  // is written only for the sites that need it)
+  if (cudaMemset(b->knn, 0, sizeof(unsigned) * knn_cap) != cudaSuccess) {
+    set_error("batch: memset failed");
+    free_batch(b);
+    return VGB_ERR_CUDA;
   }
   // concatenated inputs
   {

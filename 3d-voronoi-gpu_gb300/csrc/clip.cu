@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
     const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss,
     const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ out_list,
-    int* __restrict__ out_count, int* __restrict__ work, const CellStore store) {
+    int* __restrict__ out_count, int* __restrict__ work, const CellStore store, int k_tier) {
   __shared__ SiteSmem<SL> smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -183,9 +183,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
 #define PD(f) (BATCHED ? probs[pidx].f : lone.f)
     const int K = PD(K);
     const float4 seed = sites[s];
+    // a stored cell that reached its security radius within the first K1
+    // neighbours (all its row has when the kNN ran in tiers) needs no more
+    const int resume = stored >> 16;
+    const bool stored_secure = stored != 0 && resume == 0 && ((stored >> 8) & 1) == 0;
+    const int Kload = (stored_secure && k_tier > 0 && k_tier < K) ? k_tier : K;
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
-    for (int j = lane; j < K; j += WARP) {
+    for (int j = lane; j < Kload; j += WARP) {
       float4 B = sites[krow[j]];
       float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
       float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
@@ -435,10 +440,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       // the plane sequence: bisectors until the security radius, the six
       // domain-box faces, or the tet's four faces
       const bool bis = job == 0 || !CELL_TET;
-      const int pbeg = job == 1 ? 4 + K + BOX_PLANES : bis ? 4 : 0;
-      const int pend = job == 1 ? pbeg + BOX_PLANES : (job == 0 && stored) ? pbeg : bis ? 4 + K : 4;
+      // a stored cell is final, or (resume) was built from the first K1
+      // bisectors and goes on from there
+      const int resume_at = (job == 0 && stored) ? resume : 0;
+      const int pbeg = job == 1 ? 4 + K + BOX_PLANES : resume_at ? resume_at : bis ? 4 : 0;
+      const int pend = job == 1 ? pbeg + BOX_PLANES : (job == 0 && stored) ? (resume_at ? 4 + K : pbeg)
+                     : bis ? 4 + K : 4;
       int state = 0;  // 0 kept, 1 empty, 2 dropped
-      bool secmiss = (job == 0 && stored) ? (stored >> 8) != 0 : bis;
+      bool secmiss = (job == 0 && stored && !resume_at) ? ((stored >> 8) & 1) != 0 : bis;
       // counters of the sequence, packed: planes (bits 0-7), cuts (8-15),
       // vertex-vs-plane tests (16-31); at most 144 planes of 96 vertices
       unsigned seq_cnt = 0u;
@@ -661,7 +670,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
     unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
     const unsigned* __restrict__ field_sat, int* __restrict__ work, int* __restrict__ out_list,
-    int* __restrict__ out_count, int kmax, const CellStore store) {
+    int* __restrict__ out_count, int kmax, const CellStore store, int k_tier, int* __restrict__ deep_list,
+    int* __restrict__ deep_count) {
   constexpr int NG = WARP / G;
   __shared__ BuildSmem<G * SL> smem_all[CLIP_WARPS * NG];
   extern __shared__ float4 build_planes[];
@@ -682,11 +692,13 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int pidx = (BATCHED && has) ? site_prob[s] : 0;
 #define PD(f) (BATCHED ? probs[pidx].f : lone.f)
     const int K = has ? PD(K) : 0;
+    // with a tier, only the first K1 neighbour rows are computed yet
+    const int K1 = (k_tier > 0 && k_tier < K) ? k_tier : K;
     const float4 seed = has ? sites[s] : make_float4(500.f, 500.f, 500.f, 0.f);
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     if (has) {
       const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
-      for (int j = gl; j < K; j += G) {
+      for (int j = gl; j < K1; j += G) {
         const float4 B = sites[krow[j]];
         const float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
         const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
@@ -721,7 +733,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     // bisectors, nearest first, until the security radius
     bool building = has, secmiss = true;
     int pi = 4, state = 0;
-    const int pend = 4 + K;
+    const int pend = 4 + K1;
     unsigned seq_cnt = 0u;  // planes (bits 0-7), cuts (8-15), vertex-vs-plane tests (16-31)
     while (__any_sync(FULL, building)) {
       const float4 P = building ? plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
@@ -805,8 +817,13 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
         S.cnt[WC_FINAL] += (unsigned)c.nt;
       }
     }
-    // a cell handed on is stored (when it was built) for the one-warp pass
+    // a cell handed on is stored (when it was built) for the one-warp pass; a
+    // site that is not done within the tier's K1 neighbours (its security
+    // radius missed, or its cell dropped) needs its full row: it goes on the
+    // deep list, and a cell that missed its radius is stored with the plane
+    // to resume from
     const bool keep = has && !interior && state == 0;
+    const bool deep = has && !interior && K1 < K && !(state == 0 && !secmiss);
     if (store.tri) {
       int base = 0;
 #pragma unroll
@@ -820,8 +837,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
       S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
       S.cnt[WC_CONFLICT] += seq_cnt >> 16;
       if (!interior) {
-        if (store.nt) store.nt[s] = keep ? (c.nt | (secmiss ? 256 : 0)) : 0;
+        if (store.nt) store.nt[s] = keep ? (c.nt | (secmiss ? 256 : 0) | (deep ? (4 + K1) << 16 : 0)) : 0;
         out_list[atomicAdd(out_count, 1)] = s;
+        if (deep) deep_list[atomicAdd(deep_count, 1)] = s;
       }
     }
     __syncwarp();
@@ -894,13 +912,14 @@ static int build_blocks(bool batched, int kmax) {
   return b;
 }
 
-int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
+int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, const ProbDesc* probs,
                     const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
-                    const CellStore& store, cudaStream_t st) {
+                    const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
+                    cudaStream_t st) {
   if (n <= 0) return 0;
   if (g_clip_resident_blocks[0] == 0 && clip_prepare()) return -2;
   if (!cell_tet && probs) {
@@ -917,17 +936,21 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     k_clip_site<false, false, SLOTS_TET_CELL><<<(int)(want < need ? want : need), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
         nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr,
-        CellStore{});
+        CellStore{}, 0);
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
   // counters: [0] sites the first pass hands on, [1] sites the one-warp pass
-  // hands on, [2..4] the three passes' work counters; lists: [0, n) the
-  // one-warp pass's hand-offs, [n, 2n) the first pass's
+  // hands on, [2..4] the three passes' work counters, [5] the kNN's, [8] deep
+  // sites (not done within the tier's neighbours), [9] their kNN's work
+  // counter; lists: [0, n) the one-warp pass's hand-offs, [n, 2n) the first
+  // pass's, [2n, 3n) the deep sites
   const bool exact = tet_order != nullptr;
   int* const redo = lists;
   int* const rest = lists + n;
-  VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 5 * sizeof(int), st));
+  int* const deep = lists + 2 * (size_t)n;
+  const int kt = exact ? k_tier : 0;
+  VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 10 * sizeof(int), st));
   // every pass: one wave of resident blocks whose warps draw sites from a counter
   // the first pass's stored cells (exact form only)
   const CellStore cs = exact ? store : CellStore{};
@@ -936,7 +959,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
         tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, in_list, in_count, out_list,
-        out_count, work, cs);
+        out_count, work, cs, kt);
   };
   if (exact) {
     if (kmax < 1 || kmax > MAX_SITE_K) {
@@ -949,11 +972,16 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* k
     if (probs)
       k_build<true, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
           sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
-          cs);
+          cs, kt, deep, counters + 8);
     else
       k_build<false, BUILD_G, BUILD_SL><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
           sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
-          cs);
+          cs, kt, deep, counters + 8);
+    // the full rows of the deep sites, before the one-warp pass reads them
+    if (kt > 0 && kt < kmax &&
+        knn_sites_listed(sites, n, cell_start, probs, site_prob, lone, kmax, pos_of_id, knn, deep, counters + 8,
+                         counters + 9, st))
+      return -2;
   }
   const int* in_list = exact ? rest : nullptr;
   const int* in_count = exact ? counters + 0 : nullptr;

@@ -58,8 +58,8 @@ struct vgb_engine {
   float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
   float4* tet_sph = nullptr;       // exact form: tet bounding spheres (centroid-cell order)
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
-  int* redo_list = nullptr;        // cell-tet: sites handed from one clip pass to the next (2n)
-  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counter (8)
+  int* redo_list = nullptr;        // cell-tet: sites handed from one clip pass to the next, deep sites (3n)
+  int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counters (12)
   vgb::CellStore store{};          // exact form: cells the first clip pass built and handed on (by site)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
@@ -191,11 +191,14 @@ int run_pass(vgb_engine* e, int update) {
     return VGB_ERR_CUDA;
   VGB_CUDA_TRY(cudaMemcpyAsync(e->sites, e->sites_tmp, sizeof(float4) * e->n, cudaMemcpyDeviceToDevice, st));
   MARK(1);
+  const bool exact = e->field != nullptr;
+  // the exact cell-tet form computes KNN_TIER neighbours first (the rest for
+  // the sites that need them, in the clip phase)
+  const int tier = (exact && e->cfg.method == VGB_METHOD_CELL_TET && e->K > KNN_TIER) ? KNN_TIER : 0;
   if (knn_sites(e->sites, e->n, e->cell_start, nullptr, nullptr, e->prob, e->K, e->pos_of_id, e->knn, e->redo_count + 5,
-                st))
+                st, tier))
     return VGB_ERR_CUDA;
   MARK(2);
-  const bool exact = e->field != nullptr;
   if (exact && tet_reach(e->sites, e->cell_start, nullptr, nullptr, e->prob, 1, e->tet_sph, e->n_tet, e->reach,
                          e->reach_max, st))
     return VGB_ERR_CUDA;
@@ -216,7 +219,8 @@ int run_pass(vgb_engine* e, int update) {
     if (clip_site_major(e->cfg.method == VGB_METHOD_CELL_TET, e->sites, e->n, e->knn, nullptr, nullptr, e->prob,
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
-                        e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, e->store, st))
+                        e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, e->store, tier, e->cell_start,
+                        e->pos_of_id, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -357,7 +361,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 2 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 8)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 3 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 12)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT)) ||
       (rc = dalloc(&e->store.tri, exact_form ? (size_t)n_site * STORE_VERTS : 1)) ||
@@ -365,6 +369,10 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     free_engine(e);
     return rc;
   }
+  // neighbour rows start as valid indices (with the kNN in tiers a row's tail
+  // is written only for the sites that need it)
+  ce = cudaMemset(e->knn, 0, sizeof(unsigned) * (size_t)n_site * e->K);
+  if (ce != cudaSuccess) { set_error("memset: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   for (auto& ev : e->ev) {
     ce = cudaEventCreate(&ev);
     if (ce != cudaSuccess) { set_error("event: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }

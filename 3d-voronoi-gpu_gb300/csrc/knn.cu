@@ -175,7 +175,9 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
                                                         const int4* __restrict__ tets,
                                                         const int* __restrict__ q_order, int n_query,
                                                         const int* __restrict__ pos_of_id,
-                                                        unsigned* __restrict__ out, int* __restrict__ work) {
+                                                        unsigned* __restrict__ out, int* __restrict__ work,
+                                                        int k_tier, const int* __restrict__ q_list,
+                                                        const int* __restrict__ q_count) {
   __shared__ u64 buf_all[KNN_WARPS][KNN_BUF];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -194,12 +196,17 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
     }
     return cur + (int)gridDim.x * KNN_WARPS;
   };
-  for (int q = work ? next_q(0) : blockIdx.x * KNN_WARPS + wib; q < n_query; q = next_q(q)) {
+  // site queries: every site, or the sites q_list names (q_count of them)
+  const int nq = (!CENTROIDS && q_list) ? *q_count : n_query;
+  for (int q = work ? next_q(0) : blockIdx.x * KNN_WARPS + wib; q < nq; q = next_q(q)) {
+    const int qs = (!CENTROIDS && q_list) ? q_list[q] : q;
     // centroid queries belong to the lone problem
     int pq = 0;
-    const ProbDesc P = CENTROIDS ? lone : prob_for(probs, site_prob, q, lone, pq);
+    const ProbDesc P = CENTROIDS ? lone : prob_for(probs, site_prob, qs, lone, pq);
     const int dim = P.dim, cbase = P.cell_off;
-    const int K = CENTROIDS ? kq : P.K;
+    // Kr neighbours per row; the first K of them computed (k_tier caps K)
+    const int Kr = CENTROIDS ? kq : P.K;
+    const int K = (k_tier > 0 && k_tier < Kr) ? k_tier : Kr;
     const float h = 1000.f / (float)dim;
     float4 Q;
     int self = -1, orow = q;
@@ -213,8 +220,8 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
       Q.z = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), d.z), 0.25f);
       Q.w = 0.f;
     } else {
-      Q = sites[q];
-      self = q;
+      Q = sites[qs];
+      self = qs;
     }
     const int ci = grid_axis(Q.x, dim), cj = grid_axis(Q.y, dim), ck = grid_axis(Q.z, dim);
     u64 L[S];
@@ -319,7 +326,7 @@ __global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict
       warp_merge<S>(L, b, lane);
       __syncwarp();
     }
-    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * K : out + P.knn_off + (size_t)(q - P.site_off) * K;
+    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * Kr : out + P.knn_off + (size_t)(qs - P.site_off) * Kr;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int e = s * 32 + lane;
@@ -355,7 +362,7 @@ template <bool CENTROIDS>
 static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* site_prob,
                       const ProbDesc& lone, int kmax, int kq, const float4* verts, const int4* tets,
                       const int* q_order, int n_query, const int* pos_of_id, unsigned* out, int* work,
-                      cudaStream_t st) {
+                      int k_tier, const int* q_list, const int* q_count, cudaStream_t st) {
   if (kmax < 1 || kmax > 128) {
     set_error("kNN: k=%d outside [1, 128]", kmax);
     return -1;
@@ -367,24 +374,37 @@ static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc
   if (work) VGB_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   if (kmax <= 32)
     k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work);
+                                                           tets, q_order, n_query, pos_of_id, out, work,
+                                                           k_tier, q_list, q_count);
   else if (kmax <= 64)
     k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work);
+                                                           tets, q_order, n_query, pos_of_id, out, work,
+                                                           k_tier, q_list, q_count);
   else
     k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work);
+                                                           tets, q_order, n_query, pos_of_id, out, work,
+                                                           k_tier, q_list, q_count);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st) {
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st,
+              int k_tier) {
   if (n <= 0) return 0;
   k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, probs, site_prob, lone, pos_of_id);
   VGB_CUDA_TRY(cudaGetLastError());
+  const int kc = (k_tier > 0 && k_tier < kmax) ? k_tier : kmax;
+  return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kc, 0, nullptr, nullptr, nullptr, n,
+                           pos_of_id, out, work, k_tier, nullptr, nullptr, st);
+}
+
+int knn_sites_listed(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
+                     const ProbDesc& lone, int kmax, const int* pos_of_id, unsigned* out, const int* q_list,
+                     const int* q_count, int* work, cudaStream_t st) {
+  if (n <= 0) return 0;
   return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kmax, 0, nullptr, nullptr, nullptr, n,
-                           pos_of_id, out, work, st);
+                           pos_of_id, out, work, 0, q_list, q_count, st);
 }
 
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
@@ -394,7 +414,7 @@ int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start
   if (n_tet <= 0) return 0;
   const ProbDesc lone = lone_problem(n, dim, n_tet, k);
   return launch_knn<true>(sites, cell_start, nullptr, nullptr, lone, k, k, verts, tets, tet_order, n_tet, pos_of_id,
-                          out, work, st);
+                          out, work, 0, nullptr, nullptr, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -45,6 +45,10 @@ enum StatSlot : int {
 
 constexpr int WARP = 32;
 constexpr int MAX_SITE_K = 128;   // largest supported site-kNN K
+// Exact cell-tet form with K above it: the kNN first computes this many
+// neighbours per site; the sites whose cell is not done with them get their
+// full K afterwards.
+constexpr int KNN_TIER = 32;
 constexpr int MAX_TET_K = 128;    // largest supported candidates per tet
 
 // Grid of the reference (knearests.cu:19-27, :243): dim^3 cells over
@@ -165,12 +169,20 @@ int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbD
 // (lone problem).  Centroid queries come grouped by cell: tet_order /
 // tet_cell_start from tets_by_cell.  kmax: the largest K of the problems.
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
-              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st);
+              const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st,
+              int k_tier = 0);
+// The full K-lists of the sites q_list names (q_count of them, on the device);
+// pos_of_id as knn_sites left it.
+int knn_sites_listed(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
+                     const ProbDesc& lone, int kmax, const int* pos_of_id, unsigned* out, const int* q_list,
+                     const int* q_count, int* work, cudaStream_t st);
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, int* work, cudaStream_t st);
 // work (optional, 1 int): a counter the kNN warps draw queries from (one wave
 // of resident blocks, reset by the call); null deals queries round-robin.
+// k_tier > 0: only the first min(K, k_tier) neighbours of each row are
+// computed (the rows keep their K entries; the rest is left as it was).
 // Exact form: reach[q] = (distance from the centroid of the q-th tet in
 // centroid-cell order to its nearest site of the same problem) + 2 (its
 // bounding radius); reach_max_bits[p] = float bits of problem p's largest
@@ -213,20 +225,26 @@ struct CellStore {
   int* nt;        // [n]
 };
 
-int clip_site_major(bool cell_tet, const float4* sites, int n, const unsigned* knn, const ProbDesc* probs,
+int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, const ProbDesc* probs,
                     const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
                     const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
                     const unsigned char* field, const unsigned* field_sat, const int* tet_order,
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
-                    const CellStore& store, cudaStream_t st);
+                    const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
+                    cudaStream_t st);
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.  lists (2n ints) and counters (at least 5
 // ints): cell-tet scratch for the sites one pass hands to the next (the
 // lane-group first pass of the exact form, the one-warp pass, the 128-vertex
 // pass) and the passes' work counters.  The engine and the batch keep a
 // sixth int after them for the kNN's work counter.  kmax: the largest K of
-// the problems (it sizes the first pass's shared memory).
+// the problems (it sizes the first pass's shared memory).  k_tier > 0 (exact
+// form): the neighbour rows hold only their first min(K, k_tier) entries (the
+// kNN ran with that tier); the first pass builds from them, and the rows of
+// the sites it leaves unfinished are completed (knn_sites_listed, from
+// cell_start and pos_of_id) before the one-warp pass.  lists: 3n ints,
+// counters: at least 10.
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.

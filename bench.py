@@ -498,11 +498,17 @@ def accuracy_run(eng, P, K, m, iters):
         eng.sync()
         vol, mom = eng.moments()
         _, ids = eng.sites()
-        knn = eng.buffer("knn").astype(np.int64)
         pos = pre[ids]                                  # pre-update positions, this iteration's grid order
         smp = rng.choice(len(pos), m, replace=False)
-        dK = np.linalg.norm(pos[knn[smp, K - 1]] - pos[smp], axis=1)
-        r = checker.sample_cells(pos, smp, knn[smp], P.verts, P.tets, dK + 1.0)
+        # the sampled sites' K nearest (the engine's rows hold only what the
+        # cells needed when its kNN runs in tiers)
+        from scipy.spatial import cKDTree
+        dist, nb = cKDTree(pos).query(pos[smp], K + 2)
+        keep = nb != smp[:, None]                       # self excluded (by index: duplicates stay)
+        keep[keep.sum(1) > K, -1] = False
+        nbr = nb[keep].reshape(m, K)
+        dK = dist[keep].reshape(m, K)[:, K - 1]
+        r = checker.sample_cells(pos, smp, nbr, P.verts, P.tets, dK + 1.0)
         # relative error on the cells above 1e-9 of the largest sampled volume;
         # the (near-degenerate) cells below it by their absolute error, as the
         # parity tests hold them
