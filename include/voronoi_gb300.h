@@ -73,7 +73,9 @@ enum vgb_stat {
 /* Buffers readable with vgb_engine_copy_buffer. */
 enum vgb_buffer {
   VGB_BUF_SITES = 0,      /* float4[n]: x, y, z, original id (int bits), grid order */
-  VGB_BUF_KNN = 1,        /* uint32[n][site_k]: neighbours in grid order           */
+  VGB_BUF_KNN = 1,        /* uint32[n][site_k]: neighbours in grid order; in the exact
+                             cell-tet form with site_k > 32 a row is complete only for
+                             the sites whose cell needed more than its first 32     */
   VGB_BUF_CAND = 2,       /* uint32[n_tet][tet_k]: candidate sites per tet (not in the exact form) */
   VGB_BUF_CELL_START = 3, /* int32[grid_dim^3 + 1]                                  */
   VGB_BUF_SITE_START = 4, /* int32[n + 1]: start of each site's candidate tets      */
