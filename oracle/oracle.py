@@ -99,6 +99,8 @@ def knn(ref, qry=None, k: int = 64, key=None, exclude_self: bool | None = None, 
             exclude_self = True
     qry = _f32(qry)
     key = _i32(key) if key is not None else None
+    if k < 1 or k > len(ref) - (1 if exclude_self else 0):
+        raise ValueError(f"knn: k={k} with {len(ref)} points")
     nq = len(qry)
     idx = np.empty((nq, k), np.int32)
     dd = np.empty((nq, k), np.float32)
@@ -116,6 +118,8 @@ def knn_grid(ref, qry=None, k: int = 64, key=None, exclude_self: bool | None = N
             exclude_self = True
     qry = _f32(qry)
     key = _i32(key) if key is not None else None
+    if k < 1 or k > len(ref) - (1 if exclude_self else 0):
+        raise ValueError(f"knn_grid: k={k} with {len(ref)} points")
     dim = dim or grid_dim(len(ref))
     idx = np.empty((len(qry), k), np.int32)
     lib().orc_knn_grid(_p(ref), len(ref), _p(key), _p(qry), len(qry), k, int(bool(exclude_self)), dim, _p(idx),

@@ -323,3 +323,24 @@ def test_sites_on_tet_face_planes(built, meshgen, oracle, form):
         check_moments(oracle, P, g, r)
     # every site keeps its volume: none loses the pieces beside its plane
     assert abs(r["vol"].sum() / mv - 1) < 1e-4
+
+
+@pytest.mark.parametrize("n_site,K", [(40, 39), (200, 64), (3000, 128)])
+def test_exact_form_neighbour_tiers(built, meshgen, oracle, n_site, K):
+    """The exact form computes 32 neighbours first and the full K only for
+    the sites whose cell is not done with them (the first clip pass lists
+    them, the one-warp pass resumes their cell).  With K just above the tier
+    on a tiny problem nearly every site takes that path; the moments must be
+    those of the full K."""
+    pkg = built
+    P = meshgen.cube_problem(6, n_site, seed=7)
+    tk = min(128, n_site)  # every site a candidate of every tet when there are few
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, tet_k=tk, exact=True) as e:
+        e.iterate(1, update=False)
+        e.sync()
+        s4 = e.buffer("sites")
+        g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
+        g["vol"], g["mom"] = e.moments()
+    assert g["stats"]["tri_overflow"] == 0 and g["stats"]["boundary_fail"] == 0
+    r = oracle.iteration(P.sites, P.verts, P.tets, K, tk)
+    check_moments(oracle, P, by_id(g), by_id(r))
