@@ -11,28 +11,42 @@
 // once, kept in shared memory, and each candidate tet clips a copy by its
 // four faces.
 //
-// GB300 layout (site-major, one warp per site):
+// GB300 layout (site-major).  The exact form of the cell-tet method runs
+// three passes:
+//   * k_build: every site's cell built from its bisectors in a lane group of
+//     8 lanes x 4 triangle slots (32 vertices), four sites per warp on one
+//     instruction stream (group_clip); a cell that provably lies inside the
+//     mesh is finished there, every other site is listed (its cell stored as
+//     plane-id triples when it was built; the sites not done within the
+//     first kNN tier are listed again for their full neighbour rows);
+//   * k_clip_site over the listed sites (or over every site in the reference
+//     form), one warp per site, 2 slots per lane (64 vertices): the site's
+//     cell (stored, resumed, or built), its bound by the domain box when its
+//     security radius was missed, then the candidate tets;
+//   * k_clip_site with 4 slots (128 vertices) over the sites whose cell
+//     outgrew 64.
+//   The tet-cell method is k_clip_site with 3 slots (96 vertices, the
+//   reference's triangle capacity).  Within a warp or group:
 //   * the K bisector planes of the site are computed once, in coordinates
 //     relative to the site, and staged in shared memory; every candidate tet
 //     of the site reuses them;
-//   * candidate tets are first tested 32 at a time, one per lane, against the
-//     planes: a tet whose four corners are all strictly outside one bisector
-//     cannot meet the cell (the full clip would empty it at that plane).
-//     Planes come nearest first, so a lane stops as soon as the plane
-//     distance exceeds twice its tet's farthest corner;
-//   * surviving tets are clipped by the whole warp: the cell's vertices (dual
-//     triangles, three plane ids each) are spread over the lanes, three
-//     slots per lane (96 vertices, the reference's triangle capacity), with
-//     their coordinates cached in registers, so a conflict test is one 4-term
-//     dot product per vertex and a ballot;
+//   * candidate tets are first tested 32 at a time, one per lane: bounding
+//     spheres, the tet's reach, and a face of the cell (or, in the tet-cell
+//     method, a bisector) with all four corners strictly outside;
+//   * surviving tets clip a copy of the cell: its vertices (dual triangles,
+//     three plane ids each) spread over the lanes with their coordinates
+//     cached in registers, so a conflict test is one 3-FMA evaluation per
+//     vertex and a ballot;
 //   * the cavity boundary is found in parallel: a directed edge of a removed
 //     triangle is on the boundary when no other removed triangle holds its
-//     twin -- one lane per edge and a __match_any_sync on the undirected edge
-//     key; each boundary edge (a, b) becomes the new triangle (plane, a, b)
-//     -- the same triangles the reference's boundary walk produces
-//     (voronoi.cu:391-441, 479-485), in a different order.  Surviving
-//     triangles keep their slots; new ones fill the freed slots and the
-//     receiving lane computes the new vertex;
+//     twin (a __match_any_sync on the undirected edge key in the warp clip, a
+//     search of the removed triangles in the group clip); each boundary edge
+//     (a, b) becomes the new triangle (plane, a, b) -- the same triangles the
+//     reference's boundary walk produces (voronoi.cu:391-441, 479-485), in a
+//     different order.  Surviving triangles keep their slots; new ones fill
+//     the freed slots and the receiving lane computes the new vertex;
+//   * every warp (or group) draws its next site from a counter, one wave of
+//     resident blocks per pass;
 //   * moments are taken from the mean of the cell's vertices instead of the
 //     site (any apex gives the same sums; an inside apex avoids cancellation),
 //     with the edge feet computed from the edge direction n_p x n_q, which is
