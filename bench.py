@@ -83,7 +83,13 @@ DEFAULT_WORKLOAD = "torus128_uniform_1m"
 # kernels per step besides the grid sort: kNN 2, then exact form: reach, clip,
 # update; reference form: candidate kNN, candidate lists (count, scan x3,
 # fill), clip, update; plain: candidate kNN, clip, update
-LAUNCHES_PER_STEP = {"exact": 5, "cell_tet": 10, "site_major": 10, "plain": 5}
+# kernels per Lloyd iteration besides the grid sort: exact form -- position
+# map, kNN (first tier), tet reach, first clip pass, kNN of the listed sites
+# (K > 32 only), one-warp and 128-vertex clip passes, update; reference
+# cell-tet form -- position map, site kNN, centroid kNN, candidate count, scan
+# (3), fill, the two clip passes, update; tet-cell: one clip pass; plain: the
+# thread-per-pair clip and its update
+LAUNCHES_PER_STEP = {"exact": 8, "cell_tet": 11, "site_major": 10, "plain": 5}
 
 
 def grid_sort_launches(ncell: int) -> int:
@@ -459,12 +465,14 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "n_site": eng.n_site, "n_tet": eng.n_tet,
                    "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
+                   "knn_tiers": ([32, eng.site_k] if exact and args.method == "cell_tet" and eng.site_k > 32
+                                 else [eng.site_k]),
                    "form": "exact (inside cells whole, boundary cells against every tet in reach)" if exact
                            else "reference (per-tet sums over tet_k candidates)",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
                    "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
                    "parallelism": f"replicas x{world}"},
-        "gpu_launches": (LAUNCHES_PER_STEP["exact" if exact else args.method] +
+        "gpu_launches": (LAUNCHES_PER_STEP["exact" if exact else args.method] - (1 if exact and K <= 32 else 0) +
                          grid_sort_launches(eng.grid_dim ** 3)) * args.steps,
         "e2e": e2e,
         "roofline": roofline,
