@@ -179,6 +179,29 @@ def test_kn_api_matches_oracle(built, meshgen, oracle):
     assert np.array_equal(knn, r["nbr"])
 
 
+@pytest.mark.parametrize("dist,K", [("uniform", 32), ("uniform", 20), ("gaussian", 32), ("gaussian", 9)])
+def test_kn_api_large_rows(built, oracle, dist, K):
+    """Rows of at most 32 neighbours (one slot of keys per lane) at 200,000
+    sites, uniform or clustered (many sites per cell next to empty cells),
+    against the oracle's exact kNN."""
+    pkg = built
+    rng = np.random.default_rng(21)
+    n = 200_000
+    if dist == "uniform":
+        s = rng.uniform(0, 1000, (n, 3))
+    else:
+        c = rng.uniform(100, 900, (16, 3))
+        s = np.clip(c[rng.integers(0, 16, n)] + rng.normal(0, 15.0, (n, 3)), 0, 1000)
+    s = s.astype(np.float32)
+    kn = pkg.KnProblem(s, k=K)
+    kn.solve()
+    perm = kn.permutation().astype(np.int64)
+    knn = kn.knearests().astype(np.int64)
+    kn.close()
+    idx = oracle.knn_grid(s, k=K).astype(np.int64)
+    assert np.array_equal(perm[knn], idx[perm])
+
+
 @pytest.mark.parametrize("case", ["k_eq_n_minus_1", "duplicates", "outside_box", "tiny"])
 def test_edge_cases(built, meshgen, oracle, case):
     pkg = built
