@@ -430,6 +430,15 @@ def run_ours(args):
         roofline_issue = {"kernel": kname, "bound": "issue", "achieved": round(ach, 1), "peak": round(issue_peak, 1),
                           "unit": "G warp-inst/s", "frac": round(ach / issue_peak, 4),
                           "warp_instructions_per_launch": winst, "ms_per_launch": round(phases["clip"], 4)}
+    # the kNN's real bound is the same: 64-bit key selection, not HBM
+    roofline_knn_issue = None
+    kinst = profile_value("knn_sites", args.workload, "warp_instructions_per_launch")
+    if kinst:
+        ach = kinst / (phases["knn"] / 1e3) / 1e9
+        roofline_knn_issue = {"kernel": roofline_knn["kernel"], "bound": "issue", "achieved": round(ach, 1),
+                              "peak": round(issue_peak, 1), "unit": "G warp-inst/s",
+                              "frac": round(ach / issue_peak, 4), "warp_instructions_per_launch": kinst,
+                              "ms_per_launch": round(phases["knn"], 4)}
 
     accuracy = None
     if args.accuracy > 0 and rank == 0:
@@ -477,7 +486,7 @@ def run_ours(args):
         "e2e": e2e,
         "roofline": roofline,
         "roofline_knn": roofline_knn,
-        "roofline_issue": roofline_issue,
+        "roofline_issue": roofline_issue, "roofline_knn_issue": roofline_knn_issue,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "pairs_per_s": round(pairs_per_s, 1),
         "clipped_pairs_per_s": round(stats["clipped"] * value / world, 1),
