@@ -30,11 +30,11 @@ STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
 STAT_NAMES = ["candidates", "culled", "clipped", "empty", "contrib", "security_miss", "tri_overflow",
               "boundary_fail", "planes", "clips", "final_vertices", "conflict_tests", "cull_tests",
-              "new_vertices", "interior", "redo"]
+              "new_vertices", "interior", "redo", "needs_exact"]
 PHASE_NAMES = ["grid", "knn", "candidates", "site_lists", "clip", "update"]
 BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6}
 METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}
-STAT_COUNT = 16
+STAT_COUNT = 17
 
 
 class VoronoiError(RuntimeError):
@@ -52,7 +52,7 @@ def build(force: bool = False) -> Path:
 
 class _Config(C.Structure):
     _fields_ = [("site_k", C.c_int), ("tet_k", C.c_int), ("grid_dim", C.c_int), ("method", C.c_int),
-                ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int)]
+                ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int), ("robust_predicates", C.c_int)]
 
 
 class _KnProblem(C.Structure):
@@ -167,10 +167,15 @@ class Engine:
     stores sites in grid order.  exact=True (cell-tet): cells inside the mesh
     are taken whole and the others are clipped by every tet within reach,
     instead of the reference's per-tet sums over tet_k candidates.
+    robust_predicates=True: vertex-vs-plane tests within 1e-4 of zero (relative
+    to their terms) are decided by exact determinant signs (the reference's
+    arithmetic filter, with an exact fallback); degenerate inputs such as
+    lattice sites come out whole.
     """
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
-                 method: str = "cell_tet", use_graph: bool = True, device: int = 0, exact: bool = False):
+                 method: str = "cell_tet", use_graph: bool = True, device: int = 0, exact: bool = False,
+                 robust_predicates: bool = False):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -182,6 +187,7 @@ class Engine:
         cfg.site_k, cfg.tet_k, cfg.grid_dim = site_k, tet_k, grid_dim
         cfg.method, cfg.use_graph, cfg.device = METHODS[method], int(use_graph), device
         cfg.exact = int(exact)
+        cfg.robust_predicates = int(robust_predicates)
         h = C.c_void_p()
         _check(L.vgb_engine_create(C.byref(h), C.byref(cfg), _p(self._verts), len(self._verts), _p(self._tets),
                                    len(self._tets), _p(s), len(s)), "vgb_engine_create")
@@ -298,7 +304,7 @@ class Batch:
     """
 
     def __init__(self, problems, site_k: int = 0, tune_grid: bool = True, use_graph: bool = True,
-                 device: int = 0):
+                 device: int = 0, robust_predicates: bool = False):
         L = lib()
         self._v = [_f32(v) for v, _, _ in problems]
         self._t = [np.ascontiguousarray(t, dtype=np.int32) for _, t, _ in problems]
@@ -317,6 +323,7 @@ class Batch:
         L.vgb_config_init(C.byref(cfg))
         cfg.site_k, cfg.grid_dim = site_k, 0 if tune_grid else 1
         cfg.method, cfg.use_graph, cfg.device, cfg.exact = METHODS["cell_tet"], int(use_graph), device, 1
+        cfg.robust_predicates = int(robust_predicates)
         h = C.c_void_p()
         _check(L.vgb_batch_create(C.byref(h), C.byref(cfg), P, vp_arr, nv, tp_arr, nt, sp_arr, ns),
                "vgb_batch_create")

@@ -31,7 +31,8 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xco
                   f"-I{INC}", f"-I{CSRC}"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", f"-I{INC}", f"-I{CSRC}"]
 
-LIB_CU = ["grid.cu", "knn.cu", "clip.cu", "clip_plain.cu", "engine.cu", "kn_api.cu", "noalloc.cu", "batch.cu"]
+LIB_CU = ["grid.cu", "knn.cu", "clip.cu", "clip_robust.cu", "clip_plain.cu", "engine.cu", "kn_api.cu", "noalloc.cu",
+          "batch.cu"]
 LIB_CPP = ["voronoi_api.cpp", "mesh_field.cpp"]
 
 

@@ -171,7 +171,7 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   if (clip_site_major(true, b->sites, b->n, b->knn, b->d_probs, b->site_prob, none, b->verts, b->tets, nullptr,
                       nullptr, b->mom, b->stats, b->field, b->field_sat, b->tet_order, b->tet_cell_start, b->tet_sph,
                       b->reach, b->reach_max, count_secmiss ? b->secmiss : nullptr, b->redo_list, b->redo_count,
-                      b->kmax, b->store, tier, b->cell_start, b->pos_of_id, st))
+                      b->kmax, b->store, tier, b->cell_start, b->pos_of_id, b->cfg.robust_predicates != 0, st))
     return VGB_ERR_CUDA;
   if (finish_sites(b->sites, b->n, b->mom, update, st)) return VGB_ERR_CUDA;
   return VGB_OK;

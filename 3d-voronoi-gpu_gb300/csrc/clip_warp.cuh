@@ -13,6 +13,7 @@
 #pragma once
 
 #include "vgb_common.cuh"
+#include "exact_pred.cuh"
 
 namespace vgb {
 
@@ -61,6 +62,52 @@ __device__ __forceinline__ float3 vertex_of(float4 a, float4 b, float4 c) {
 }
 // |x|^2, with the same rounding everywhere
 __device__ __forceinline__ float norm2_rn(float3 x) { return dot3_rn(x.x, x.y, x.z, x.x, x.y, x.z); }
+
+// Robust-predicate variants (the ROBUST instantiations of the clips).  A
+// vertex-vs-plane test is decided in float unless |P(v)| lies within
+// ROBUST_BAND of the sum of its terms' magnitudes; such a test is decided
+// exactly from the vertex's three planes (exact_pred.cuh), a vertex on the
+// plane kept.  With exact decisions a cut never crosses an edge that lies in
+// the cutting plane, so a new vertex is where the plane crosses an edge
+// between a removed and a kept vertex; its three planes can still nearly
+// share a line (a plane through a cell edge within rounding), where a float
+// determinant cancels, so new vertices are computed in double.  The exact
+// and double paths are out of line.
+constexpr float ROBUST_BAND = 1e-4f;
+
+static __device__ __noinline__ bool exact_outside(float4 A, float4 B, float4 C, float4 P) {
+  return exact_side(A, B, C, P) < 0;
+}
+
+// Is the vertex (x, y, z) of triangle tri strictly outside P?  nexact
+// (shared, may be null) counts the exact decisions.
+__device__ __forceinline__ bool vertex_outside_robust(float4 P, float x, float y, float z, unsigned tri,
+                                                      const float4* planes, unsigned* nexact) {
+  const float e = plane_eval(P, x, y, z);
+  const float sc = fabsf(P.x * x) + fabsf(P.y * y) + fabsf(P.z * z) + fabsf(P.w);
+  if (fabsf(e) > ROBUST_BAND * sc) return e < 0.f;
+  if (nexact) atomicAdd(nexact, 1u);
+  return exact_outside(planes[tri & 0xffu], planes[(tri >> 8) & 0xffu], planes[(tri >> 16) & 0xffu], P);
+}
+
+// Vertex of three planes in double (float inputs: every product exact).
+static __device__ __noinline__ float3 vertex_of_d(float4 a, float4 b, float4 c) {
+  const double ax = a.x, ay = a.y, az = a.z, aw = a.w, bx = b.x, by = b.y, bz = b.z, bw = b.w;
+  const double cx = c.x, cy = c.y, cz = c.z, cw = c.w;
+  const double bcx = by * cz - bz * cy, bcy = bz * cx - bx * cz, bcz = bx * cy - by * cx;
+  const double cax = cy * az - cz * ay, cay = cz * ax - cx * az, caz = cx * ay - cy * ax;
+  const double abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+  const double det = ax * bcx + ay * bcy + az * bcz;
+  const double s = -1.0 / det;
+  return make_float3((float)(s * (aw * bcx + bw * cax + cw * abx)), (float)(s * (aw * bcy + bw * cay + cw * aby)),
+                     (float)(s * (aw * bcz + bw * caz + cw * abz)));
+}
+
+// The robust variants compute every new vertex in double: a float vertex
+// from planes that nearly share a line carries an error up to its condition
+// number times float rounding, enough to put a later float test on the wrong
+// side of the exact band.
+__device__ __forceinline__ float3 vertex_of_robust(float4 a, float4 b, float4 c) { return vertex_of_d(a, b, c); }
 
 // Plane through three points, normal (p1-p0)x(p2-p0): positive inside a
 // positively oriented tet for the faces (c,b,d), (a,c,d), (b,a,d), (a,b,c)
@@ -139,9 +186,10 @@ __device__ __forceinline__ bool cavity_disk_small(int R, int nb) { return nb == 
 // bedge are 32 SL-entry scratch arrays of
 // the warp.  need_r2: keep c.r2 (the largest |vertex|^2) current; callers that
 // never read it skip the warp reduction.
-template <int SL>
+template <int SL, bool ROBUST = false>
 __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
-                                         unsigned* conf, unsigned* bedge, const int lane, const bool need_r2) {
+                                         unsigned* conf, unsigned* bedge, const int lane, const bool need_r2,
+                                         unsigned* nexact = nullptr) {
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   unsigned m[SL];
   int nconf = 0;
@@ -149,7 +197,9 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
   for (int k = 0; k < SL; ++k) {
     m[k] = 0u;
     if (c.vm[k]) {
-      bool cf = (c.vm[k] & lane_bit) && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
+      bool cf = (c.vm[k] & lane_bit) &&
+                (ROBUST ? vertex_outside_robust(P, c.vx[k], c.vy[k], c.vz[k], c.tri[k], planes, nexact)
+                        : plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f);
       m[k] = __ballot_sync(FULL, cf);
       nconf += __popc(m[k]);
     }
@@ -254,7 +304,7 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
     if (recv) {
       unsigned E = bedge[r];
       unsigned ea = E & 0xffu, eb = E >> 8;
-      float3 x = vertex_of(P, planes[ea], planes[eb]);
+      float3 x = ROBUST ? vertex_of_robust(P, planes[ea], planes[eb]) : vertex_of(P, planes[ea], planes[eb]);
       c.tri[k] = pack_tri(pidx, ea, eb);
       c.vx[k] = x.x;
       c.vy[k] = x.y;
@@ -423,10 +473,10 @@ __device__ __forceinline__ unsigned group_min_u(unsigned v, int gid) {
 // and end exactly one boundary edge; the fan (pidx, a, b) fills freed slots.
 // Returns the group's result; the cell is changed only on CLIP_CUT.  conf and
 // bedge: the group's G SL-entry scratch arrays.
-template <int G, int SL>
+template <int G, int SL, bool ROBUST = false>
 __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
                                           unsigned* conf, unsigned* bedge, const int gl, const int gbase,
-                                          const int gid, const bool act) {
+                                          const int gid, const bool act, unsigned* nexact = nullptr) {
   constexpr int CAP = G * SL;
   const unsigned lb = 1u << gl, ltm = lb - 1u;
   unsigned m[SL];
@@ -435,7 +485,9 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
 #pragma unroll
   for (int k = 0; k < SL; ++k) {
     const bool live = c.vm[k] & lb;
-    const bool cf = act && live && plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f;
+    const bool cf = act && live &&
+                    (ROBUST ? vertex_outside_robust(P, c.vx[k], c.vy[k], c.vz[k], c.tri[k], planes, nexact)
+                            : plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f);
     m[k] = group_ballot<G>(cf, gbase);
     nconf += __popc(m[k]);
     if (live && !cf) lm = fmaxf(lm, c.vw[k]);
@@ -523,7 +575,7 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
     if (recv) {
       const unsigned Ed = bedge[r];
       const unsigned ea = Ed & 0xffu, eb = Ed >> 8;
-      const float3 x = vertex_of(P, planes[ea], planes[eb]);
+      const float3 x = ROBUST ? vertex_of_robust(P, planes[ea], planes[eb]) : vertex_of(P, planes[ea], planes[eb]);
       c.tri[k] = pack_tri(pidx, ea, eb);
       c.vx[k] = x.x;
       c.vy[k] = x.y;

@@ -220,7 +220,7 @@ int run_pass(vgb_engine* e, int update) {
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
                         e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, e->store, tier, e->cell_start,
-                        e->pos_of_id, st))
+                        e->pos_of_id, e->cfg.robust_predicates != 0, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -278,6 +278,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->use_graph = 1;
   cfg->device = 0;
   cfg->exact = 0;
+  cfg->robust_predicates = 0;
 }
 
 const char* vgb_last_error(void) { return vgb::last_error(); }

@@ -40,7 +40,8 @@ enum StatSlot : int {
   STAT_NEW_VERTICES = 13,    // vertices created by clipping
   STAT_INTERIOR = 14,        // sites whose whole cell lies inside the mesh (taken whole)
   STAT_REDO = 15,            // sites redone with the larger cell capacity (their cell outgrew 64 vertices)
-  STAT_COUNT = 16
+  STAT_NEEDS_EXACT = 16,     // vertex-vs-plane tests decided by the exact determinants (robust predicates)
+  STAT_COUNT = 17
 };
 
 constexpr int WARP = 32;
@@ -232,7 +233,8 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, co
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                     const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
-                    cudaStream_t st);
+                    bool robust, cudaStream_t st);
+// robust: the robust-predicate instantiation of the kernels.
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.  lists (2n ints) and counters (at least 5
 // ints): cell-tet scratch for the sites one pass hands to the next (the

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cstdlib>
 #include <cstdio>
 #include <fstream>
 #include <iomanip>
@@ -53,6 +54,10 @@ extern "C" int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const
   if (cfg.site_k >= n_site) cfg.site_k = n_site - 1;
   cfg.tet_k = preferred_tet_k;
   cfg.use_graph = 0;  // per-phase timing for record.csv
+  // the reference turns its arithmetic filter on at compile time
+  // (USE_ARITHMETIC_FILTER, params.h:27-32); here VGB_ROBUST_PREDICATES=1 in
+  // the environment turns on the filter with its exact fallback
+  if (const char* r = std::getenv("VGB_ROBUST_PREDICATES")) cfg.robust_predicates = std::atoi(r) != 0;
   vgb_engine* e = nullptr;
   int rc = vgb_engine_create(&e, &cfg, vertices, n_vert, indices, n_tet, aos.data(), n_site);
   if (rc) return rc;

@@ -335,7 +335,7 @@ def run_ours(args):
     K = w["K"]
     exact = args.method == "cell_tet" and not args.reference_form
     eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
-                     exact=exact)
+                     exact=exact, robust_predicates=args.robust_predicates)
     K = eng.site_k  # the autotuned K when the workload asks for one
 
     def barrier():
@@ -476,6 +476,7 @@ def run_ours(args):
                    "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
                    "knn_tiers": ([32, eng.site_k] if exact and args.method == "cell_tet" and eng.site_k > 32
                                  else [eng.site_k]),
+                   "robust_predicates": bool(args.robust_predicates),
                    "form": "exact (inside cells whole, boundary cells against every tet in reach)" if exact
                            else "reference (per-tet sums over tet_k candidates)",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
@@ -696,6 +697,9 @@ def main():
     ap.add_argument("--reference-form", action="store_true",
                     help="cell-tet: sum every cell over its tet_k candidate tets, as the reference does, instead "
                          "of the exact form (cells inside the mesh whole, the rest against every tet in reach)")
+    ap.add_argument("--robust-predicates", action="store_true",
+                    help="decide near-zero vertex-vs-plane tests by exact determinant signs (off by default, "
+                         "as the reference's arithmetic filter is)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", type=int, default=0, metavar="M",
                     help="after timing, report per-iteration error against the FP64 oracle on M sampled sites")

@@ -61,7 +61,10 @@ enum vgb_stat {
   VGB_STAT_NEW_VERTICES = 13,   /* vertices created by clipping                       */
   VGB_STAT_INTERIOR = 14,       /* sites whose whole cell lies inside the mesh        */
   VGB_STAT_REDO = 15,           /* sites redone at 128 vertices (outgrew 64)          */
-  VGB_STAT_COUNT = 16
+  VGB_STAT_NEEDS_EXACT = 16,    /* robust_predicates: vertex-vs-plane tests decided by
+                                   the exact determinants (the reference's status
+                                   needs_exact_predicates, voronoi_defs.h:10)          */
+  VGB_STAT_COUNT = 17
 };
 
 /* Clip kernels. */
@@ -97,12 +100,20 @@ typedef struct vgb_config {
                    provably lies inside the mesh is taken whole, any other cell is
                    clipped by every tet within its reach (no tet_k heuristic, no
                    candidate kNN).  Both agree when the candidate sets are complete. */
+  int robust_predicates; /* cell-tet and tet-cell forms.  0: float vertex-vs-plane tests
+                   (the reference as shipped).  1: a test whose float value lies within
+                   1e-4 of the scale of its terms is decided by the exact signs of the
+                   4x4 and 3x3 plane determinants, a vertex on the plane kept -- the
+                   reference's arithmetic filter (params.h:27-32, voronoi.cu:285-303),
+                   which gives up on such a cell, with the exact fallback it lacks.
+                   Makes degenerate inputs (sites on a regular lattice, cospherical
+                   neighbours) come out whole.                                      */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;
 
 /* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0,
- * exact 0 (the reference's per-tet sums over tet_k candidates). */
+ * exact 0 (the reference's per-tet sums over tet_k candidates), robust_predicates 0. */
 void vgb_config_init(vgb_config* cfg);
 
 /* One-line description of a CUDA device (name, SMs, memory) into buf. */

@@ -367,3 +367,75 @@ def test_exact_form_neighbour_tiers(built, meshgen, oracle, n_site, K):
     assert g["stats"]["tri_overflow"] == 0 and g["stats"]["boundary_fail"] == 0
     r = oracle.iteration(P.sites, P.verts, P.tets, K, tk)
     check_moments(oracle, P, by_id(g), by_id(r))
+
+
+def lattice_problem(meshgen, n_side=8):
+    """Sites on a regular n_side^3 lattice of exact float32 values (62.5 +
+    125 i for 8) in the 6^3 Kuhn cube; each cell is its lattice box clipped
+    to the mesh's bounding cube.  Returns the problem and those volumes and
+    barycentres."""
+    P0 = meshgen.cube_problem(6, 10, seed=1)
+    h = 1000.0 / n_side
+    g1 = h / 2 + h * np.arange(n_side)
+    s = np.stack(np.meshgrid(g1, g1, g1, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    P = meshgen.Problem(f"lattice{n_side}", P0.verts, P0.tets, s)
+    lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
+    a = np.maximum(s.astype(np.float64) - h / 2, lo)
+    b = np.minimum(s.astype(np.float64) + h / 2, hi)
+    return P, np.prod(b - a, axis=1), (a + b) / 2
+
+
+def run_engine_by_id(pkg, P, **kw):
+    with pkg.Engine(P.verts, P.tets, P.sites, **kw) as e:
+        e.iterate(1, update=False)
+        e.sync()
+        s4 = e.buffer("sites")
+        g = dict(ids=s4[:, 3].copy().view(np.int32), stats=e.stats())
+        g["vol"], g["mom"] = e.moments()
+    return by_id(g)
+
+
+@pytest.mark.parametrize("form", ["exact", "cell_tet", "site_major"])
+def test_regular_lattice_sites_robust_predicates(built, meshgen, oracle, form):
+    """Sites on a regular lattice: every cell vertex lies exactly on the
+    bisectors of the edge and corner neighbours, so float tests against those
+    planes come out either way, and a cut can then build a vertex from three
+    planes through one line (the reference's algorithm in double -- the
+    oracle -- returns NaN for most of these cells).  With robust predicates
+    such tests are decided exactly, a vertex on the plane kept, and every
+    cell is its lattice box clipped to the mesh: the regular-lattice known
+    answer."""
+    pkg = built
+    P, vref, bref = lattice_problem(meshgen)
+    kw = dict(site_k=64, robust_predicates=True)
+    if form == "exact":
+        kw.update(exact=True)
+    else:
+        kw.update(method=form, tet_k=128)
+    g = run_engine_by_id(pkg, P, **kw)
+    st = g["stats"]
+    assert st["boundary_fail"] == 0 and st["tri_overflow"] == 0
+    assert st["needs_exact"] > 0
+    assert np.isfinite(g["vol"]).all() and np.isfinite(g["mom"]).all()
+    rel = np.abs(g["vol"] - vref) / vref
+    assert rel.max() < VOL_RTOL, (rel.max(), int(np.argmax(rel)))
+    diag = float(np.linalg.norm(P.verts.max(0).astype(np.float64) - P.verts.min(0)))
+    err = np.linalg.norm(g["mom"] / g["vol"][:, None] - bref, axis=1).max() / diag
+    assert err < BARY_DIAG_TOL, err
+    mv = oracle.mesh_volume(P.verts, P.tets)
+    assert abs(g["vol"].sum() - mv) / mv < TOTAL_RTOL
+
+
+def test_robust_predicates_leave_general_inputs_unchanged(built, meshgen, oracle):
+    """On sites in general position the exact path decides only tests the
+    float path already decides right: the moments still match the oracle,
+    and agree with the float path's to float rounding."""
+    pkg = built
+    P = meshgen.cube_problem(10, 4000, seed=11)
+    a = run_engine_by_id(pkg, P, site_k=64, exact=True)
+    b = run_engine_by_id(pkg, P, site_k=64, exact=True, robust_predicates=True)
+    assert b["stats"]["boundary_fail"] == 0
+    r = oracle.iteration(P.sites, P.verts, P.tets, 64, 100)
+    check_moments(oracle, P, b, by_id(r))
+    big = a["vol"] > 1e-9 * a["vol"].max()
+    assert (np.abs(a["vol"][big] - b["vol"][big]) / a["vol"][big]).max() < VOL_RTOL
