@@ -70,3 +70,33 @@ def test_status_values_match_reference(pkg):
     vals = dict(re.findall(r"(\w+) = (\d+)", text))
     for i, n in enumerate(pkg.STATUS_NAMES):
         assert int(vals[n]) == i
+
+
+def test_python_mirrors_match_the_c_layouts(pkg, tmp_path):
+    """The ctypes mirrors of vgb_config and kn_problem, and the stat names,
+    against the C header as a C compiler lays it out."""
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "voronoi_gb300.h"\n#include "knearests.h"\n'
+                   "int main(void) {\n"
+                   '  printf("config %zu", sizeof(vgb_config));\n'
+                   '  printf(" robust %zu exact %zu", offsetof(vgb_config, robust_predicates), '
+                   "offsetof(vgb_config, exact));\n"
+                   '  printf(" stats %d", (int)VGB_STAT_COUNT);\n'
+                   '  printf(" kn %zu knearests %zu\\n", sizeof(kn_problem), offsetof(kn_problem, d_knearests));\n'
+                   "  return 0; }\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include", str(src), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()
+    vals = {out[i]: int(out[i + 1]) for i in range(0, len(out), 2)}
+    C = pkg._Config
+    assert ctypes.sizeof(C) == vals["config"]
+    assert C.robust_predicates.offset == vals["robust"] and C.exact.offset == vals["exact"]
+    assert pkg.STAT_COUNT == vals["stats"] == len(pkg.STAT_NAMES)
+    assert ctypes.sizeof(pkg._KnProblem) == vals["kn"] and pkg._KnProblem.d_knearests.offset == vals["knearests"]
+    # the header's VGB_STAT_* order is the order of the names
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "voronoi_gb300.h").read_text(), flags=re.S)
+    stats = re.findall(r"VGB_STAT_(\w+) = (\d+)", text)
+    order = [n.lower() for n, v in sorted(stats, key=lambda t: int(t[1])) if n != "COUNT"]
+    assert order == pkg.STAT_NAMES
