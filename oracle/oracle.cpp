@@ -29,6 +29,12 @@
 //     from the edge direction (a site lying exactly on a tet face plane, which
 //     float32 lattice meshes make happen, loses volume in the shipped form).
 //     This is the accuracy oracle the GPU path is held to.
+//   ROBUST (double): FIXED with every conflict test decided by the exact sign
+//     of its 4x4 determinant (a vertex on the plane is kept) -- the exact
+//     predicates the reference's arithmetic filter asks for
+//     (needs_exact_predicates, voronoi.cu:285-303) and never evaluates.
+//     Degenerate inputs (sites on a regular lattice) then come out whole;
+//     FIXED returns NaN for most such cells.
 //
 // Distances for neighbour selection use d = fma(dz,dz, fma(dy,dy, dx*dx)) in
 // float, the contraction nvcc applies to the reference's distance expressions
@@ -90,6 +96,67 @@ template <typename R> static inline R det4(R a11, R a12, R a13, R a14, R a21, R 
   R m234 = m34 * a23 - m24 * a33 + m23 * a43;
   return (m234 * a14 - m134 * a24 + m124 * a34 - m123 * a44);
 }
+
+// Exact sign of a 4x4 determinant of doubles (ROBUST mode): Shewchuk's
+// expansion arithmetic (Two-Sum; Two-Product through fma; every partial
+// product added to a nonoverlapping expansion, so the sum is exact and its
+// sign is the sign of its largest component).  Expanded along the first two
+// rows: the 2x2 minors of each pair of rows are exact 4-term expansions.
+static inline void xs_two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  double bv = s - a, av = s - bv;
+  e = (a - av) + (b - bv);
+}
+static void xs_grow(std::vector<double>& e, double b) {
+  double q = b;
+  size_t m = 0;
+  for (size_t i = 0; i < e.size(); ++i) {
+    double s, h;
+    xs_two_sum(q, e[i], s, h);
+    q = s;
+    if (h != 0.0) e[m++] = h;
+  }
+  e.resize(m);
+  if (q != 0.0) e.push_back(q);
+}
+static void xs_add_prod(std::vector<double>& e, double a, double b) {  // e += a * b
+  double p = a * b;
+  double q = std::fma(a, b, -p);
+  if (q != 0.0) xs_grow(e, q);
+  if (p != 0.0) xs_grow(e, p);
+}
+static int exact_det4_sign(const double m[4][4]) {
+  // Laplace along rows 0-1: sum over column pairs (i<j) of
+  // (-1)^(i+j+1) * minor01(i,j) * minor23(complement)
+  static const int P[6][4] = {{0, 1, 2, 3}, {0, 2, 1, 3}, {0, 3, 1, 2}, {1, 2, 0, 3}, {1, 3, 0, 2}, {2, 3, 0, 1}};
+  static const double S[6] = {1, -1, 1, 1, -1, 1};
+  std::vector<double> e;
+  for (int t = 0; t < 6; ++t) {
+    const int i = P[t][0], j = P[t][1], k = P[t][2], l = P[t][3];
+    // minor01 = m0i m1j - m0j m1i, minor23 = m2k m3l - m2l m3k: the product
+    // is the sum of the four cross products of their terms
+    const double a[2] = {m[0][i] * S[t], -m[0][j] * S[t]};
+    const double b[2] = {m[1][j], m[1][i]};
+    const double c[2] = {m[2][k], -m[2][l]};
+    const double d[2] = {m[3][l], m[3][k]};
+    for (int u = 0; u < 2; ++u)
+      for (int v = 0; v < 2; ++v) {
+        // (a_u * b_u) * (c_v * d_v), each factor an exact 2-term product
+        const double p1 = a[u] * b[u], q1 = std::fma(a[u], b[u], -p1);
+        const double p2 = c[v] * d[v], q2 = std::fma(c[v], d[v], -p2);
+        xs_add_prod(e, p1, p2);
+        xs_add_prod(e, p1, q2);
+        xs_add_prod(e, q1, p2);
+        xs_add_prod(e, q1, q2);
+      }
+  }
+  for (size_t n = e.size(); n > 0; --n)
+    if (e[n - 1] != 0.0) return e[n - 1] > 0.0 ? 1 : -1;
+  return 0;
+}
+
+// ROBUST mode switch: set before the parallel loops, read-only inside them.
+static bool g_exact_predicates = false;
 
 // Plane through three points, normal (p1-p0)x(p2-p0), positive inside for a
 // positively oriented tet (voronoi.cu:119-123, 41-46).
@@ -206,6 +273,13 @@ struct Cell {
   bool in_conflict(int t, V4<R> e) const {
     if (ctr) ctr->conflict_tests++;
     V4<R> p1 = pl[tr[t][0]], p2 = pl[tr[t][1]], p3 = pl[tr[t][2]];
+    if (!SHIPPED && g_exact_predicates) {
+      const double m[4][4] = {{(double)p1.x, (double)p2.x, (double)p3.x, (double)e.x},
+                              {(double)p1.y, (double)p2.y, (double)p3.y, (double)e.y},
+                              {(double)p1.z, (double)p2.z, (double)p3.z, (double)e.z},
+                              {(double)p1.w, (double)p2.w, (double)p3.w, (double)e.w}};
+      return exact_det4_sign(m) > 0;
+    }
     R d = det4(p1.x, p2.x, p3.x, e.x, p1.y, p2.y, p3.y, e.y, p1.z, p2.z, p3.z, e.z, p1.w, p2.w, p3.w, e.w);
     return d > R(0);
   }
@@ -616,7 +690,8 @@ int orc_tet_k(int n_site, int n_tet, int preferred) {
 //   nbr    : n x K, K nearest neighbours of each site, self excluded
 //   verts  : nv x 3, tets: nt x 4 (positively oriented)
 //   cand   : nt x tk, candidate sites per tet
-//   mode   : 0 = SHIPPED float (pair order, float sums), 1 = FIXED double
+//   mode   : 0 = SHIPPED float (pair order, float sums), 1 = FIXED double,
+//            2 = ROBUST (FIXED with exact conflict tests)
 // Outputs per site: vol[n], mom[3n] (first moment = sum vol * barycentre),
 // status histogram hist[7] of (non-)contributing pairs (contributing pairs are
 // counted in hist[7 + s]); pair_status[nt*tk] optional.
@@ -627,6 +702,7 @@ void orc_tet_cell(int mode, const float* sites, int n, const int* nbr, int K, co
   std::memset(mom, 0, sizeof(double) * 3 * n);
   for (int i = 0; i < 14; ++i) hist[i] = 0;
   long long npairs = (long long)nt * tk;
+  g_exact_predicates = mode == 2;
   if (mode == 0) {
     // Serial, in the reference's thread order, float accumulation.
     std::vector<float> fv(n, 0.f), fm(3 * (size_t)n, 0.f);
@@ -732,6 +808,7 @@ void orc_cell_tet(int mode, const float* sites, int n, const int* nbr, int K, co
   std::memset(mom, 0, sizeof(double) * 3 * n);
   for (int i = 0; i < 14; ++i) hist[i] = 0;
   long long npairs = (long long)nt * tk;
+  g_exact_predicates = mode == 2;
   auto run = [&](auto tag) {
     using R = typename decltype(tag)::first_type;
     constexpr bool SH = decltype(tag)::second_type::value;

@@ -20,7 +20,7 @@ LIB = BUILD / "liboracle.so"
 STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
 
-SHIPPED, FIXED = 0, 1
+SHIPPED, FIXED, ROBUST = 0, 1, 2
 
 
 def build(force: bool = False) -> Path:

@@ -48,3 +48,19 @@ def oracle():
 
 def golden(name):
     return np.load(GOLDEN / name)
+
+
+def lattice_problem(meshgen, n_side=8):
+    """Sites on a regular n_side^3 lattice of exact float32 values (62.5 +
+    125 i for 8) in the 6^3 Kuhn cube; each cell is its lattice box clipped
+    to the mesh's bounding cube.  Returns the problem and those volumes and
+    barycentres."""
+    P0 = meshgen.cube_problem(6, 10, seed=1)
+    h = 1000.0 / n_side
+    g1 = h / 2 + h * np.arange(n_side)
+    s = np.stack(np.meshgrid(g1, g1, g1, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    P = meshgen.Problem(f"lattice{n_side}", P0.verts, P0.tets, s)
+    lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
+    a = np.maximum(s.astype(np.float64) - h / 2, lo)
+    b = np.minimum(s.astype(np.float64) + h / 2, hi)
+    return P, np.prod(b - a, axis=1), (a + b) / 2

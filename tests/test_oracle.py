@@ -3,7 +3,7 @@ kernels (tests/golden/make_golden.py), and its known-answer properties."""
 import numpy as np
 import pytest
 
-from conftest import REF_DATA, golden
+from conftest import REF_DATA, golden, lattice_problem
 
 
 def _status_hist(res):
@@ -171,6 +171,36 @@ def test_fixed_oracle_lattice_sites_have_equal_cells(meshgen, oracle):
     assert abs(f["vol"].sum() / oracle.mesh_volume(P.verts, P.tets) - 1) < 1e-9
     bary = f["mom"] / f["vol"][:, None]
     assert np.allclose(bary, s, atol=0.05)
+
+
+@pytest.mark.parametrize("method", ["tet_cell", "cell_tet"])
+def test_robust_oracle_exact_lattice_known_answer(meshgen, oracle, method):
+    """The exact lattice itself (no perturbation).  The FIXED oracle -- the
+    reference's algorithm in double -- loses most cells (NaN: its float
+    conflict tests come out either way on the on-plane vertices and a cut
+    then builds a vertex from three planes through one line); the ROBUST
+    mode decides every conflict test by the exact sign of its determinant
+    and gives each cell its lattice box clipped to the mesh."""
+    P, vref, bref = lattice_problem(meshgen)
+    nbr, _ = oracle.knn(P.sites, None, 64)
+    cand, _ = oracle.knn(P.sites, oracle.tet_centroids(P.verts, P.tets), 128, exclude_self=False)
+    run = getattr(oracle, method)
+    f = run(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
+    assert not (np.isfinite(f["vol"]).all() and np.allclose(f["vol"], vref, rtol=1e-6))
+    r = run(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.ROBUST)
+    assert np.allclose(r["vol"], vref, rtol=1e-12, atol=0)
+    assert np.allclose(r["mom"] / r["vol"][:, None], bref, rtol=0, atol=1e-9)
+
+
+def test_robust_oracle_equals_fixed_in_general_position(meshgen, oracle):
+    """Sites in general position: exact conflict tests change nothing."""
+    P = meshgen.cube_problem(8, 1500, seed=7)
+    nbr, _ = oracle.knn(P.sites, None, 64)
+    cand, _ = oracle.knn(P.sites, oracle.tet_centroids(P.verts, P.tets), 50, exclude_self=False)
+    f = oracle.tet_cell(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
+    r = oracle.tet_cell(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.ROBUST)
+    assert np.allclose(r["vol"], f["vol"], rtol=1e-12, atol=1e-9)
+    assert np.allclose(r["mom"], f["mom"], rtol=1e-12, atol=1e-6)
 
 
 def test_lloyd_update_matches_reference(meshgen, oracle):
