@@ -1,11 +1,13 @@
-// VolumeVoronoiGPU <tet_mesh.tet|vtk> <sites.xyz> <nb_iter> [k] [--site-k=N]
+// VolumeVoronoiGPU <tet_mesh.tet|vtk> <sites.xyz> <nb_iter> [k] [--site-k=N] [--robust-predicates]
 //
 // The reference's CLI (test_voronoi.cu:190-227): loads the mesh and
 // normalises it to [0,1000]^3 (test_voronoi.cu:14-121), loads the sites
 // (test_voronoi.cu:135-147; SoA when fewer than 14000 sites, as
 // KNEARESTS_MIN_N in params.h:1 selects), runs nb_iter Lloyd iterations with
 // tet_k = k (0 or absent: the heuristic), and writes out.xyz, record.csv and
-// iter_<i>.xyz.  --site-k sets the neighbours per site (default 90).
+// iter_<i>.xyz.  --site-k sets the neighbours per site (default 90);
+// --robust-predicates turns on the arithmetic filter with its exact fallback
+// (the reference's compile-time USE_ARITHMETIC_FILTER, params.h:27-32).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -115,11 +117,13 @@ int main(int argc, char** argv) {
   int site_k = 90;
   for (int i = 1; i < argc; ++i) {
     if (!std::strncmp(argv[i], "--site-k=", 9)) site_k = std::atoi(argv[i] + 9);
+    else if (!std::strcmp(argv[i], "--robust-predicates")) setenv("VGB_ROBUST_PREDICATES", "1", 1);
     else pos.push_back(argv[i]);
   }
   if (pos.size() < 3) {
     std::cerr << "Usage: " << argv[0] << " <tet_mesh.tet/vtk> <sites_file.xyz> <nb_iter> <k (optional)>"
-              << " [--site-k=N] (e.g.: " << argv[0] << " joint.tet joint.xyz 120 0)" << std::endl;
+              << " [--site-k=N] [--robust-predicates] (e.g.: " << argv[0] << " joint.tet joint.xyz 120 0)"
+              << std::endl;
     return 1;
   }
   char desc[256];
