@@ -173,20 +173,23 @@ def test_fixed_oracle_lattice_sites_have_equal_cells(meshgen, oracle):
     assert np.allclose(bary, s, atol=0.05)
 
 
+@pytest.mark.parametrize("n_side", [4, 5, 8])
 @pytest.mark.parametrize("method", ["tet_cell", "cell_tet"])
-def test_robust_oracle_exact_lattice_known_answer(meshgen, oracle, method):
+def test_robust_oracle_exact_lattice_known_answer(meshgen, oracle, method, n_side):
     """The exact lattice itself (no perturbation).  The FIXED oracle -- the
     reference's algorithm in double -- loses most cells (NaN: its float
     conflict tests come out either way on the on-plane vertices and a cut
     then builds a vertex from three planes through one line); the ROBUST
     mode decides every conflict test by the exact sign of its determinant
     and gives each cell its lattice box clipped to the mesh."""
-    P, vref, bref = lattice_problem(meshgen)
-    nbr, _ = oracle.knn(P.sites, None, 64)
-    cand, _ = oracle.knn(P.sites, oracle.tet_centroids(P.verts, P.tets), 128, exclude_self=False)
+    P, vref, bref = lattice_problem(meshgen, n_side)
+    n = len(P.sites)
+    nbr, _ = oracle.knn(P.sites, None, min(64, n - 1))
+    cand, _ = oracle.knn(P.sites, oracle.tet_centroids(P.verts, P.tets), min(128, n), exclude_self=False)
     run = getattr(oracle, method)
-    f = run(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
-    assert not (np.isfinite(f["vol"]).all() and np.allclose(f["vol"], vref, rtol=1e-6))
+    if n_side == 8:
+        f = run(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.FIXED)
+        assert not (np.isfinite(f["vol"]).all() and np.allclose(f["vol"], vref, rtol=1e-6))
     r = run(P.sites, nbr, P.verts, P.tets, cand, mode=oracle.ROBUST)
     assert np.allclose(r["vol"], vref, rtol=1e-12, atol=0)
     assert np.allclose(r["mom"] / r["vol"][:, None], bref, rtol=0, atol=1e-9)
