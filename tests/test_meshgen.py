@@ -45,3 +45,27 @@ def test_xyz_round_trip(meshgen, tmp_path):
     back = meshgen.read_xyz(str(f))
     assert back.shape == s.shape
     assert np.allclose(back, s, rtol=0, atol=1e-3)
+
+
+def test_large_cube_generator_equals_general_one(meshgen):
+    """The 256^3 configuration uses kuhn_cube_large (no vertex
+    de-duplication, int32); on a small grid it gives kuhn_cube's mesh."""
+    n = 7
+    p_small, t_small = meshgen.kuhn_grid(
+        np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1).reshape(-1, 3), n)[1:]
+    p_large, t_large = meshgen.kuhn_cube_large(n)
+    assert np.allclose(p_small, p_large.astype(np.float64), rtol=0, atol=1e-7)
+    assert (meshgen.orient(p_large.astype(np.float64), t_large.astype(np.int64)) > 0).all()
+    key = lambda t: np.unique(np.sort(np.asarray(t, np.int64), axis=1), axis=0)
+    assert np.array_equal(key(t_small), key(t_large))
+
+
+def test_gradient_sites_density(meshgen):
+    """Density along x rising linearly 1 -> 4: mean x = (1/2 + a/3) / (1 + a/2)
+    with a = 3, and the last tenth of x holds (1 + 0.95 a) / (1 + 0.05 a)
+    times the sites of the first (the densities at the bins' centres)."""
+    s = meshgen.gradient_sites(400_000, np.random.default_rng(5))
+    assert s.min() >= 0 and s.max() <= 1
+    assert abs(s[:, 0].mean() - 0.6) < 3e-3
+    h = np.histogram(s[:, 0], bins=10, range=(0, 1))[0]
+    assert abs(h[-1] / h[0] - (1 + 3 * 0.95) / (1 + 3 * 0.05)) < 0.1
