@@ -69,3 +69,18 @@ def test_gradient_sites_density(meshgen):
     assert abs(s[:, 0].mean() - 0.6) < 3e-3
     h = np.histogram(s[:, 0], bins=10, range=(0, 1))[0]
     assert abs(h[-1] / h[0] - (1 + 3 * 0.95) / (1 + 3 * 0.05)) < 0.1
+
+
+def test_batch_problems_within_their_ranges(meshgen):
+    """The batched configuration's problems: Kuhn cubes of side n in [4, 48]
+    with jittered interiors (every tet still positive), site counts in
+    [500, 200000], sites inside each cube."""
+    probs = meshgen.batch_problems(n_prob=5, seed=4)
+    assert len(probs) == 5
+    for P in probs:
+        n = round((len(P.tets) / 6) ** (1 / 3))
+        assert 4 <= n <= 48 and len(P.tets) == 6 * n ** 3
+        assert 500 <= len(P.sites) <= 200_000
+        v = P.verts.astype(np.float64)
+        assert (meshgen.orient(v, P.tets.astype(np.int64)) > 0).all()
+        assert (P.sites >= P.verts.min(0)).all() and (P.sites <= P.verts.max(0)).all()
