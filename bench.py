@@ -3,7 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--method cell_tet|site_major|plain]
-                    [--reference-form] [--accuracy M] [--no-cpu-baseline]
+                    [--reference-form] [--robust-predicates] [--accuracy M] [--no-cpu-baseline]
 
 A step is one Lloyd iteration of the path over the whole site set: grid sort,
 site kNN, per-tet reach, clipped cells (cell-tet method, exact form: cells
@@ -16,14 +16,17 @@ reference's heuristic gives tet_k = 60 for the reference form).  Inputs are
 generated (seeded) on the host, then resident in HBM; the working set
 (neighbour lists, tet records) is several times the 129 MB L2, so no flush is
 needed between steps.  --workload batch256_kuhn runs the batched form (256
-independent problems per launch).  --accuracy M adds the per-iteration error
+independent problems per launch).  --robust-predicates runs the clip's
+robust-predicate instantiation (exact decisions of near-zero vertex-vs-plane
+tests, double-precision vertices).  --accuracy M adds the per-iteration error
 of M sampled cells against the FP64 oracle.
 
 Printed (rank 0, one JSON line): value = Lloyd iter/s with inputs resident
 (CUDA events on the engine stream around exactly K steps, after W warm-up
 steps), e2e = the same through vgb_engine_step_host with page-locked host
 buffers (site positions in and out every step), the roofline of the clip
-kernel (FP32) and of the site kNN (HBM), the reference's own CPU kernels on a
+kernel (FP32) and of the site kNN (HBM) with their instruction-issue
+rooflines, the reference's own CPU kernels on a
 bounded sample (cpu_baseline), and the SM clocks sampled during the timed
 region.  With --gpus N > 1 (torchrun), each rank runs an independent replica
 of the workload on its own GPU; value sums the replicas' iterations over the
