@@ -30,11 +30,15 @@ STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates", "no_intersection"]
 STAT_NAMES = ["candidates", "culled", "clipped", "empty", "contrib", "security_miss", "tri_overflow",
               "boundary_fail", "planes", "clips", "final_vertices", "conflict_tests", "cull_tests",
-              "new_vertices", "interior", "redo", "needs_exact"]
+              "new_vertices", "interior", "redo", "needs_exact", "completed", "unresolved"]
 PHASE_NAMES = ["grid", "knn", "candidates", "site_lists", "clip", "update"]
-BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6}
+BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "site_tets": 5, "moments": 6,
+           "site_flags": 7}
+# per-site outcome bits of a cell-tet pass (buffer "site_flags")
+SITE_HANDED, SITE_SECMISS, SITE_INTERIOR, SITE_REDO, SITE_DROPPED, SITE_COMPLETED, SITE_UNRESOLVED = (
+    1, 2, 4, 8, 16, 32, 64)
 METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}
-STAT_COUNT = 17
+STAT_COUNT = 19
 
 
 class VoronoiError(RuntimeError):
@@ -266,7 +270,8 @@ class Engine:
         which = BUFFERS[name]
         nbytes = lib().vgb_engine_buffer_bytes(self._h, which)
         dt = {"sites": np.float32, "knn": np.uint32, "cand": np.uint32, "cell_start": np.int32,
-              "site_start": np.int32, "site_tets": np.int32, "moments": np.float64}[name]
+              "site_start": np.int32, "site_tets": np.int32, "moments": np.float64,
+              "site_flags": np.uint8}[name]
         out = np.empty(nbytes // np.dtype(dt).itemsize, dt)
         _check(lib().vgb_engine_copy_buffer(self._h, which, _p(out), nbytes), "vgb_engine_copy_buffer")
         if name == "sites":

@@ -27,13 +27,15 @@ LIB = OUT / "libvoronoi_gb300.so"
 CLI = OUT / "VolumeVoronoiGPU"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# VGB_NVCC_FLAGS: extra nvcc flags for tuning builds, e.g. -DVGB_CLIP_MIN_BLOCKS=6
+# (the clip kernels' resident blocks per SM); empty for the release build.
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-                  f"-I{INC}", f"-I{CSRC}"]
+                  f"-I{INC}", f"-I{CSRC}"] + os.environ.get("VGB_NVCC_FLAGS", "").split()
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", f"-I{INC}", f"-I{CSRC}"]
 
 LIB_CU = ["grid.cu", "knn.cu", "clip.cu", "clip_robust.cu", "clip_plain.cu", "engine.cu", "kn_api.cu", "noalloc.cu",
           "batch.cu"]
-LIB_CPP = ["voronoi_api.cpp", "mesh_field.cpp"]
+LIB_CPP = ["voronoi_api.cpp", "mesh_field.cpp", "kn_cxx.cpp"]
 
 
 def _nvcc() -> str:

@@ -345,7 +345,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       (rc = balloc(&b->stats, VGB_STAT_COUNT)) || (rc = balloc(&b->field, f_off)) ||
       (rc = balloc(&b->field_sat, q_off)) || (rc = balloc(&b->reach, b->n_tet)) ||
       (rc = balloc(&b->tet_sph, b->n_tet)) || (rc = balloc(&b->reach_max, n_prob)) ||
-      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 3 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 12)) ||
+      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 5 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 12)) ||
       (rc = balloc(&b->store.tri, (size_t)b->n * vgb::STORE_VERTS)) || (rc = balloc(&b->store.nt, b->n))) {
     free_batch(b);
     return rc;

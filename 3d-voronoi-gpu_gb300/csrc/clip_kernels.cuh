@@ -74,28 +74,78 @@ namespace vgb {
 
 constexpr int CLIP_WARPS = 4;
 constexpr int BOX_PLANES = 6;
+// Resident blocks per SM the clip kernels are compiled for (the register
+// budget per thread is 65536 / (CLIP_WARPS * 32 * blocks)).
+#ifndef VGB_CLIP_MIN_BLOCKS
+#define VGB_CLIP_MIN_BLOCKS 8
+#endif
+#ifndef VGB_BUILD_MIN_BLOCKS
+#define VGB_BUILD_MIN_BLOCKS 8
+#endif
 
 enum WarpCount : int {
   WC_CAND = 0, WC_CULLED, WC_CLIPPED, WC_EMPTY, WC_CONTRIB, WC_SECMISS, WC_OVERFLOW, WC_BOUNDARY, WC_PLANES,
-  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_REDO, WC_EXACT, WC_N
+  WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_REDO, WC_EXACT, WC_COMPLETED,
+  WC_UNRESOLVED, WC_N
 };
+// Each per-warp count goes to the counter slot of the same index.
+static_assert(WC_CAND == STAT_CANDIDATES && WC_CULLED == STAT_CULLED && WC_CLIPPED == STAT_CLIPPED &&
+                  WC_EMPTY == STAT_EMPTY && WC_CONTRIB == STAT_CONTRIB && WC_SECMISS == STAT_SECURITY_MISS &&
+                  WC_OVERFLOW == STAT_TRI_OVERFLOW && WC_BOUNDARY == STAT_BOUNDARY_FAIL && WC_PLANES == STAT_PLANES &&
+                  WC_CLIPS == STAT_CLIPS && WC_FINAL == STAT_FINAL_VERTICES && WC_CONFLICT == STAT_CONFLICT_TESTS &&
+                  WC_CULLTESTS == STAT_CULL_TESTS && WC_NEWV == STAT_NEW_VERTICES && WC_INTERIOR == STAT_INTERIOR &&
+                  WC_REDO == STAT_REDO && WC_EXACT == STAT_NEEDS_EXACT && WC_COMPLETED == STAT_COMPLETED &&
+                  WC_UNRESOLVED == STAT_UNRESOLVED && WC_N == STAT_COUNT,
+              "per-warp counts and counter slots in the same order");
+__device__ __forceinline__ int stat_slot(int w) { return w; }
 
-template <int SL>
+// Plane slots of a site's shared state: 0..3 tet faces, 4+j bisector j,
+// 4+K+b start-cube face b, 4+K+6+b domain-box face b; the completion pass
+// adds the planes of the sites it finds after them, up to 256 (plane ids are
+// 8 bits).
+constexpr int SITE_PLANES = 4 + MAX_SITE_K + 2 * BOX_PLANES;
+constexpr int COMPLETE_PLANES = 256;
+
+template <int SL, int NPLANE = SITE_PLANES>
 struct SiteSmem {
-  float4 plane[4 + MAX_SITE_K + 2 * BOX_PLANES];  // 0..3 tet faces, 4+j bisector j, 4+K+b start-cube
-                                                  // face b, 4+K+6+b domain-box face b
+  float4 plane[NPLANE];                           // see SITE_PLANES
   unsigned conf[(WARP * SL)];                     // clip scratch: removed triangles
   unsigned bedge[(WARP * SL)];                    // clip scratch: boundary edges
   unsigned queue[WARP];                       // surviving candidate tets of a chunk
   float4 corner[4];                           // corners of the tet being clipped
   unsigned cnt[WC_N];                         // per-warp counters (lane 0 writes)
-  unsigned char faces[4 + MAX_SITE_K + BOX_PLANES];  // cell-tet: plane ids bounding the site's cell
+  unsigned char faces[NPLANE];                // cell-tet: plane ids bounding the site's cell
   unsigned mtri[(WARP * SL)];                     // cell-tet: the site's cell
   float4 mv[(WARP * SL)];
   unsigned mvm[SL];
   int mnt;
   float mr2;
+  // warp-uniform state of the site that is read rarely, kept here rather
+  // than in registers: the candidate scan's row range (x-runs i0..i1 of rows
+  // j0 + r % nj, k0 + r / nj, nseg of them) and the compensated sums of the
+  // site's volume and first moment (hi parts 0-3, lo parts 4-7; lane 0)
+  int scan[6];  // nseg, nj, i0, i1, j0, k0
+  float acc[8];
+  // the candidate scan's position (current row seg, its remaining range
+  // [base, se)), the cell's radius Rc, the number of its bounding planes in
+  // `faces`, the site's stored-cell word and its outcome bits
+  int seg, base, se, nfaces, stored;
+  float Rc;
+  unsigned site_flags;
+  float4 seed;  // the site (read where needed rather than held in registers)
+  // squared radius of the site's pieces (cell ^ tet) so far, when its K
+  // neighbours missed the security radius; in the completion pass, the
+  // bound its earlier pass left
+  float pr2;
 };
+
+// Compensated add (TwoSum) of x into the pair (hi, lo) in shared memory.
+__device__ __forceinline__ void comp_add(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bp = s - hi;
+  lo += (hi - (s - bp)) + (x - bp);
+  hi = s;
+}
 
 // Bounding box of the cell's vertices (site-relative), over the warp: float
 // bits mapped to an order-preserving unsigned key for the integer reductions.
@@ -127,8 +177,8 @@ __device__ __forceinline__ void cell_bounds(const WarpCell<SL>& c, int lane, flo
 
 // The site's cell into its shared copy, which the box bound and every tet
 // clip start from.
-template <int SL>
-__device__ __forceinline__ void store_master(const WarpCell<SL>& c, SiteSmem<SL>& S, int lane) {
+template <int SL, int NP>
+__device__ __forceinline__ void store_master(const WarpCell<SL>& c, SiteSmem<SL, NP>& S, int lane) {
   const unsigned lane_bit = 1u << lane;
 #pragma unroll
   for (int k = 0; k < SL; ++k)
@@ -159,8 +209,15 @@ __device__ __forceinline__ void store_master(const WarpCell<SL>& c, SiteSmem<SL>
 //     reached (voronoi.cu:679-697): the cell-tet build and the tet-cell
 //     method's per-tet cells;
 //   * tet faces 0 .. 3: the cell-tet method's per-tet clip.
-template <bool CELL_TET, bool BATCHED, int SL, bool ROBUST>
-__global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
+//
+// Exact form: a cell whose K neighbours missed its security radius is exact
+// where it meets the mesh when its pieces (cell ^ tet) lie within half the
+// K-th neighbour's distance -- no site beyond can cut them.  Otherwise the
+// site goes on the completion list with the squared radius of its pieces,
+// and the completion pass (COMPLETE) clips its cell by every site within
+// twice that radius beyond its K nearest before it clips the tets again.
+template <bool CELL_TET, bool BATCHED, int SL, bool ROBUST, bool COMPLETE = false>
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 : VGB_CLIP_MIN_BLOCKS) k_clip_site(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
     const int4* __restrict__ tets, const int* __restrict__ site_start, const int* __restrict__ site_tets,
@@ -169,14 +226,17 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
     const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss,
     const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ out_list,
-    int* __restrict__ out_count, int* __restrict__ work, const CellStore store, int k_tier) {
-  __shared__ SiteSmem<SL> smem_all[CLIP_WARPS];
+    int* __restrict__ out_count, int* __restrict__ work, const CellStore store, int k_tier,
+    const int* __restrict__ cell_start, int* __restrict__ esc_list, float* __restrict__ esc_r2,
+    int* __restrict__ esc_count) {
+  constexpr int NPLANE = COMPLETE ? COMPLETE_PLANES : SITE_PLANES;
+  constexpr int PWORDS = (NPLANE + 31) / 32;
+  __shared__ SiteSmem<SL, NPLANE> smem_all[CLIP_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  SiteSmem<SL>& S = smem_all[wib];
+  SiteSmem<SL, NPLANE>& S = smem_all[wib];
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   if (lane < WC_N) S.cnt[lane] = 0u;
-  unsigned cull_lane = 0;  // per-lane tet-vs-plane tests of the culling pass
   const bool exact = CELL_TET && tet_order != nullptr;
   __syncwarp();
 
@@ -198,7 +258,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const int s = in_list ? in_list[it] : it;
     bool abandon = false;
     // the cell the first pass built, when it stored one
-    const int stored = (CELL_TET && store.nt) ? store.nt[s] : 0;
+    if (lane == 0) S.stored = (CELL_TET && store.nt) ? store.nt[s] : 0;
+    __syncwarp();
+    const int stored0 = S.stored;
     // the site's problem; its descriptor fields are read where used (from
     // global memory or the kernel parameters) rather than held in registers
     const int pidx = BATCHED ? site_prob[s] : 0;
@@ -207,8 +269,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     const float4 seed = sites[s];
     // a stored cell that reached its security radius within the first K1
     // neighbours (all its row has when the kNN ran in tiers) needs no more
-    const int resume = stored >> 16;
-    const bool stored_secure = stored != 0 && resume == 0 && ((stored >> 8) & 1) == 0;
+    const bool stored_secure = stored0 != 0 && (stored0 >> 16) == 0 && ((stored0 >> 8) & 1) == 0;
     const int Kload = (stored_secure && k_tier > 0 && k_tier < K) ? k_tier : K;
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
@@ -228,12 +289,12 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     // cell that can meet a tet: it gives the security radius and the culling
     // radius, while the cube-start cell is what the tets clip.
     constexpr float lo = -0.1f, hi = 1000.1f;
-    auto cube_half = [&]() {
-      return fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
-                   fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
+    auto cube_half = [&](float4 p) {
+      return fmaxf(fmaxf(fmaxf(p.x - lo, hi - p.x), fmaxf(p.y - lo, hi - p.y)), fmaxf(p.z - lo, hi - p.z)) + 1.f;
     };
+    if (lane == 0) S.seed = seed;
     if (CELL_TET) {
-      const float L = cube_half();
+      const float L = cube_half(seed);
       if (lane < BOX_PLANES) {
         const int ax = lane >> 1;
         const float sgn = (lane & 1) ? -1.f : 1.f;
@@ -248,16 +309,27 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
     }
     __syncwarp();
 
-    CompSum V, MX, MY, MZ;  // site-relative volume and first moment
-    float Rc = 0.f;
-    int nfaces = 0;
+    if (lane < 8) S.acc[lane] = 0.f;  // site-relative volume and first moment
+    // outcome bits of the site (cell-tet method): this pass built its cell
+    if (lane == 0) {
+      S.site_flags = SITE_HANDED | (SL > 2 ? SITE_REDO : 0);
+      S.pr2 = COMPLETE ? esc_r2[it] : 0.f;
+      S.Rc = 0.f;
+      S.nfaces = 0;
+      S.seg = -1;
+      S.base = 0;
+      S.se = 0;
+    }
     // jobs: 0 build the site's cell; 1 bound it by the domain box (when its
     // security radius was not reached); 2 clip the next candidate tet
     int job = CELL_TET ? 0 : 2;
     // candidate scan: segments of a tet list, 32 tets per chunk
-    int nseg = 0, nj = 1, i0 = 0, i1 = 0, j0 = 0, k0 = 0;
-    int seg = -1, base = 0, se = 0, qi = 0, nsurv = 0;
-    if (!CELL_TET) nseg = 1;
+    int qi = 0, nsurv = 0;
+    if (lane == 0) {
+      S.scan[0] = CELL_TET ? 0 : 1;
+      S.scan[1] = 1;
+    }
+    __syncwarp();
 
     while (true) {
       // ---------------------------------------------------------------
@@ -265,9 +337,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       // for the box bound, or the next surviving candidate
       WarpCell<SL> c;
       cell_clear(c);
-      if (job == 0 && stored) {
+      if (job == 0 && S.stored) {
         // its vertices from its plane triples, the evaluation that made them
-        const int nt0 = stored & 255;
+        const int nt0 = S.stored & 255;
         float lm = 0.f;
 #pragma unroll
         for (int k = 0; k < SL; ++k) {
@@ -289,7 +361,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         c.nt = nt0;
         c.r2 = warp_max_nonneg(lm);
       } else if (job == 0) {
-        const float L = cube_half();
+        const float L = cube_half(S.seed);
         if (lane < 8) {
           // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
           // ordered so each dual triangle has a negative normal determinant
@@ -319,21 +391,34 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       } else {
         // refill the queue from the next chunk(s) of candidates
         while (qi >= nsurv) {
+          const int base = S.base, se = S.se;
           if (base >= se) {
-            if (++seg >= nseg) break;
+            const int seg = S.seg + 1;
+            __syncwarp();
+            if (seg >= S.scan[0]) break;
+            int b0, b1;
             if (exact) {
-              const int pd = PD(dim);
-              const int row = PD(cell_off) + pd * ((j0 + seg % nj) + pd * (k0 + seg / nj));
-              base = tet_cell_start[i0 + row];
-              se = tet_cell_start[i1 + row + 1];
+              const int pd = PD(dim), nj = S.scan[1];
+              const int row = PD(cell_off) + pd * ((S.scan[4] + seg % nj) + pd * (S.scan[5] + seg / nj));
+              b0 = tet_cell_start[S.scan[2] + row];
+              b1 = tet_cell_start[S.scan[3] + row + 1];
             } else {
-              base = site_start[s];
-              se = site_start[s + 1];
+              b0 = site_start[s];
+              b1 = site_start[s + 1];
             }
+            if (lane == 0) {
+              S.seg = seg;
+              S.base = b0;
+              S.se = b1;
+            }
+            __syncwarp();
             continue;
           }
           const int idx = base + lane;
           const bool valid = idx < se;
+          const float Rc = S.Rc;
+          const float4 seed = S.seed;
+          unsigned cull_lane = 0;  // this lane's tet-vs-plane tests
           int t = -1;
           float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
           bool alive = valid;
@@ -367,7 +452,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
             }
             // a tet whose four corners are strictly outside one face of the
             // cell cannot meet it
-            for (int f = 0; f < nfaces; ++f) {
+            for (int f = 0, nf = S.nfaces; f < nf; ++f) {
               if (!__any_sync(FULL, alive)) break;
               const float4 P = S.plane[S.faces[f]];
               if (alive) {
@@ -405,12 +490,15 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           nsurv = __popc(survivors);
           qi = 0;
           if (alive) S.queue[__popc(survivors & lt_mask)] = (unsigned)t;
+          const unsigned cull_warp = __reduce_add_sync(FULL, cull_lane);
+          __syncwarp();
           if (lane == 0) {
             S.cnt[WC_CAND] += (unsigned)nvalid;
             S.cnt[WC_CULLED] += (unsigned)(nvalid - nsurv);
             S.cnt[WC_CLIPPED] += (unsigned)nsurv;
+            S.cnt[WC_CULLTESTS] += cull_warp;
+            S.base = base + WARP;
           }
-          base += WARP;
           __syncwarp();
         }
         if (qi >= nsurv) break;  // no candidate left
@@ -419,6 +507,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           const int4 q = tets[tq];
           const int vi = lane == 0 ? q.x : lane == 1 ? q.y : lane == 2 ? q.z : q.w;
           const float4 p = verts[vi];
+          const float4 seed = S.seed;
           S.corner[lane] = make_float4(p.x - seed.x, p.y - seed.y, p.z - seed.z, 0.f);
         }
         __syncwarp();
@@ -465,12 +554,13 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       const bool bis = job == 0 || !CELL_TET;
       // a stored cell is final, or (resume) was built from the first K1
       // bisectors and goes on from there
-      const int resume_at = (job == 0 && stored) ? resume : 0;
+      const int stored = job == 0 ? S.stored : 0;
+      const int resume_at = stored ? stored >> 16 : 0;
       const int pbeg = job == 1 ? 4 + K + BOX_PLANES : resume_at ? resume_at : bis ? 4 : 0;
-      const int pend = job == 1 ? pbeg + BOX_PLANES : (job == 0 && stored) ? (resume_at ? 4 + K : pbeg)
+      const int pend = job == 1 ? pbeg + BOX_PLANES : stored ? (resume_at ? 4 + K : pbeg)
                      : bis ? 4 + K : 4;
       int state = 0;  // 0 kept, 1 empty, 2 dropped
-      bool secmiss = (job == 0 && stored && !resume_at) ? ((stored >> 8) & 1) != 0 : bis;
+      bool secmiss = (stored && !resume_at) ? ((stored >> 8) & 1) != 0 : bis;
       // counters of the sequence, packed: planes (bits 0-7), cuts (8-15),
       // vertex-vs-plane tests (16-31); at most 144 planes of 96 vertices
       unsigned seq_cnt = 0u;
@@ -479,7 +569,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         const float4 P = S.plane[pi];
         seq_cnt += 1u + ((unsigned)c.nt << 16);
         const int r = warp_clip<SL, ROBUST>(c, P, (unsigned)pi, S.plane, S.conf, S.bedge, lane, need_r2,
-                                            S.cnt + WC_EXACT);
+                                            S.cnt + WC_NEWV, S.cnt + WC_EXACT);
         if (r == CLIP_EMPTY) { state = 1; break; }
         if (r == CLIP_OVERFLOW && out_list) {
           abandon = true;
@@ -501,11 +591,16 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       }
       if (abandon) break;
       if (job == 2 && bis && state == 0 && secmiss && lane == 0) S.cnt[WC_SECMISS]++;
+      // the completion pass keeps the earlier moments of a site that loses a piece
+      if (COMPLETE && job == 2 && state == 2 && lane == 0) S.site_flags |= SITE_UNRESOLVED;
 
       // ---------------------------------------------------------------
       bool take = state == 0, interior = false;
       if (job == 0) {
-        if (state != 0) break;  // the site's cell failed: no tet is clipped
+        if (state != 0) {  // the site's cell failed: no tet is clipped
+          if (state == 2 && lane == 0) S.site_flags |= SITE_DROPPED;
+          break;
+        }
         if (secmiss) {
           // the box bound and the tets start from the cell's shared copy
           store_master(c, S, lane);
@@ -535,11 +630,125 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         }
         // |K-th neighbour - site|^2 > 4 max|v - site|^2 over the bounded cell
         const bool secmiss = build_miss && !(2.f * S.plane[4 + K - 1].w > 4.f * c.r2);
-        if (secmiss && lane == 0) {
-          S.cnt[WC_SECMISS]++;
-          if (prob_secmiss) atomicAdd(prob_secmiss + pidx, 1u);
+        bool cdone = false;  // completion pass: the cell was completed
+        if (COMPLETE) {
+          // Clip the cell by every site within 2R (R: the bound of its pieces
+          // from the earlier pass) that is not among its K nearest: after
+          // that no site can cut its pieces.  Such a site z (|z| >= |z_K|)
+          // can only remove a vertex v with |v| >= |z_K| / 2, and removes it
+          // when z . v > |z|^2 / 2 (site-relative): those far vertices are
+          // kept in shared memory (S.mv, free until the cell is stored) and
+          // each lane tests its candidate against them.  The site grid's
+          // x-runs are read ring by ring around the site's row, 32 sites at
+          // a time; the candidates that remove a far vertex clip the cell one
+          // by one, each cut taking the lowest plane slot that no vertex of
+          // the cell refers to any more.
+          const float4 seed = S.seed;
+          const unsigned* kr = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
+          const float4 zK = sites[kr[K - 1]];
+          const float dK2 = dist2(seed, zK);
+          const int idK = site_id(zK), self = site_id(seed);
+          const float R = __fmaf_rn(sqrtf(S.pr2), 1.001f, 0.01f);
+          const float lim = 4.f * R * R;
+          const float far2 = 0.249f * dK2;
+          const int dim = PD(dim), cbase = PD(cell_off);
+          const int i0 = grid_axis(seed.x - 2.f * R, dim), i1 = grid_axis(seed.x + 2.f * R, dim);
+          const int j0 = grid_axis(seed.y - 2.f * R, dim), j1 = grid_axis(seed.y + 2.f * R, dim);
+          const int k0 = grid_axis(seed.z - 2.f * R, dim), k1 = grid_axis(seed.z + 2.f * R, dim);
+          const int cj = grid_axis(seed.y, dim), ck = grid_axis(seed.z, dim);
+          const int rmax = max(max(cj - j0, j1 - cj), max(ck - k0, k1 - ck));
+          const int first_free = 4 + K + 2 * BOX_PLANES;  // slots below: the site's own planes
+          int nxt = first_free;
+          bool fail = state != 0;
+          // the far vertices of the current cell into S.mv[0, nfar)
+          auto gather_far = [&]() {
+            int nf = 0;
+#pragma unroll
+            for (int k = 0; k < SL; ++k) {
+              const bool f = (c.vm[k] & lane_bit) && c.vw[k] >= far2;
+              const unsigned fm = __ballot_sync(FULL, f);
+              if (f) S.mv[nf + __popc(fm & lt_mask)] = make_float4(c.vx[k], c.vy[k], c.vz[k], c.vw[k]);
+              nf += __popc(fm);
+            }
+            __syncwarp();
+            return nf;
+          };
+          int nfar = fail ? 0 : gather_far();
+          for (int ring = 0; ring <= rmax && !fail && nfar > 0; ++ring)
+            for (int kk = max(k0, ck - ring); kk <= min(k1, ck + ring) && !fail && nfar > 0; ++kk)
+              for (int jj = max(j0, cj - ring); jj <= min(j1, cj + ring) && !fail && nfar > 0; ++jj) {
+                if (max(abs(jj - cj), abs(kk - ck)) != ring) continue;
+                const int row = cbase + dim * (jj + dim * kk);
+                const int e = cell_start[row + i1 + 1];
+                for (int b0 = cell_start[row + i0]; b0 < e && !fail && nfar > 0; b0 += WARP) {
+                  const int idx = b0 + lane;
+                  bool cand = false;
+                  float4 P = make_float4(0.f, 0.f, 0.f, 0.f);
+                  if (idx < e) {
+                    const float4 z = sites[idx];
+                    const float d2 = dist2(seed, z);
+                    const int id = site_id(z);
+                    const float bx = z.x - seed.x, by = z.y - seed.y, bz = z.z - seed.z;
+                    const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
+                    P = make_float4(-bx, -by, -bz, 0.5f * bb);
+                    if (id != self && d2 < lim && (d2 > dK2 || (d2 == dK2 && id > idK))) {
+                      // does its bisector remove a far vertex? (z . v > |z|^2 / 2,
+                      // with a margin that keeps every true one)
+                      const float tol = 1e-5f * bb;
+                      for (int f = 0; f < nfar && !cand; ++f) {
+                        const float4 v = S.mv[f];
+                        cand = fmaf(bx, v.x, fmaf(by, v.y, bz * v.z)) > 0.5f * bb - tol;
+                      }
+                    }
+                  }
+                  for (unsigned cm = __ballot_sync(FULL, cand); cm != 0u && !fail; cm &= cm - 1u) {
+                    const int src = __ffs(cm) - 1;
+                    const float4 Q = make_float4(__shfl_sync(FULL, P.x, src), __shfl_sync(FULL, P.y, src),
+                                                 __shfl_sync(FULL, P.z, src), __shfl_sync(FULL, P.w, src));
+                    if (lane == 0) S.plane[nxt] = Q;
+                    __syncwarp();
+                    const int r = warp_clip<SL, ROBUST>(c, Q, (unsigned)nxt, S.plane, S.conf, S.bedge, lane, true,
+                                                        S.cnt + WC_NEWV, S.cnt + WC_EXACT);
+                    if (r == CLIP_CUT) {
+                      // the lowest free slot: no live vertex refers to it
+                      unsigned used[PWORDS];
+#pragma unroll
+                      for (int w = 0; w < PWORDS; ++w) used[w] = 0u;
+#pragma unroll
+                      for (int k = 0; k < SL; ++k)
+                        if (c.vm[k] & lane_bit)
+#pragma unroll
+                          for (int q = 0; q < 3; ++q) {
+                            const unsigned id = tri_at(c.tri[k], q);
+#pragma unroll
+                            for (int w = 0; w < PWORDS; ++w) used[w] |= (id >> 5) == (unsigned)w ? 1u << (id & 31u) : 0u;
+                          }
+                      nxt = NPLANE;
+#pragma unroll
+                      for (int w = PWORDS - 1; w >= 0; --w) {
+                        unsigned fr = ~__reduce_or_sync(FULL, used[w]);
+                        if (w * 32 + 31 < first_free) fr = 0u;
+                        else if (w * 32 < first_free) fr &= ~0u << (first_free - w * 32);
+                        if (fr) nxt = w * 32 + __ffs(fr) - 1;
+                      }
+                      fail = nxt >= NPLANE;
+                      // the rest of this chunk's candidates are tested again below
+                      nfar = gather_far();
+                    } else if (r != CLIP_NONE) {
+                      fail = true;
+                    }
+                  }
+                }
+              }
+          cdone = !fail;
         }
-        Rc = sqrtf(c.r2);
+        const bool miss_left = secmiss && !cdone;
+        // (counted once the site is done: a site handed to the 128-vertex
+        // pass is counted there)
+        if (secmiss && lane == 0) S.site_flags |= SITE_SECMISS;
+        const float Rc = sqrtf(c.r2);
+        if (lane == 0) S.Rc = Rc;
+        const float4 seed = S.seed;
         // A cell that provably lies inside the mesh is its own clipped cell:
         // the sum over the tets it meets of (cell ^ tet) is the cell itself.
         // When the box of field cells covering the cell holds no cell touched
@@ -550,7 +759,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
         // against the summed table.
         const float Rq = __fmaf_rn(Rc, 1.001f, 0.01f);
         const int fdim = field ? PD(fdim) : 1;
-        const int fv = field && !secmiss && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
+        const int fv = field && !miss_left && seed.x >= 0.f && seed.x <= 1000.f && seed.y >= 0.f &&
                                seed.y <= 1000.f && seed.z >= 0.f && seed.z <= 1000.f
                            ? field[PD(field_off) + grid_cell(seed.x, seed.y, seed.z, fdim)]
                            : 0;
@@ -585,55 +794,77 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
           }
         }
         take = interior;
+        if (interior && lane == 0) S.site_flags |= SITE_INTERIOR;
+        if (COMPLETE && lane == 0) S.site_flags |= cdone ? SITE_COMPLETED : SITE_UNRESOLVED;
         if (!interior) {
-          if (!build_miss) store_master(c, S, lane);
+          if (!build_miss || COMPLETE) store_master(c, S, lane);
           // the planes that bound the cell (ids present in its triangles)
-          unsigned pm[5] = {0u, 0u, 0u, 0u, 0u};
+          // (a bit per plane id, five words; selected by comparison so the
+          // words stay in registers)
+          unsigned pm[PWORDS];
+#pragma unroll
+          for (int w = 0; w < PWORDS; ++w) pm[w] = 0u;
 #pragma unroll
           for (int k = 0; k < SL; ++k)
             if (c.vm[k] & lane_bit)
 #pragma unroll
               for (int e = 0; e < 3; ++e) {
                 const unsigned id = tri_at(c.tri[k], e);
-                pm[id >> 5] |= 1u << (id & 31u);
-              }
-          nfaces = 0;
 #pragma unroll
-          for (int w = 0; w < 5; ++w) {
+                for (int w = 0; w < PWORDS; ++w) pm[w] |= (id >> 5) == (unsigned)w ? 1u << (id & 31u) : 0u;
+              }
+          int nfaces = 0;
+#pragma unroll
+          for (int w = 0; w < PWORDS; ++w) {
             const unsigned word = __reduce_or_sync(FULL, pm[w]);
             const bool has = (word >> lane) & 1u;
             const unsigned hm = __ballot_sync(FULL, has);
             if (has) S.faces[nfaces + __popc(hm & lt_mask)] = (unsigned char)(w * 32 + lane);
             nfaces += __popc(hm);
           }
+          if (lane == 0) S.nfaces = nfaces;
           // candidate tets: the site's candidate list (the reference's tet_k
           // sets), or, in the exact form, the x-runs of centroid-grid cells
           // within reach of the cell -- a tet meeting the cell has its
           // centroid within Rc + rt_max of the site, and no tet reaches
           // farther than the largest reach
-          if (exact) {
-            const int dim = PD(dim);
-            const float R = fminf(__fmaf_rn(PD(rt_max), 1.001f, Rc), __uint_as_float(reach_max_bits[pidx])) + 0.01f;
-            i0 = grid_axis(seed.x - R, dim);
-            i1 = grid_axis(seed.x + R, dim);
-            j0 = grid_axis(seed.y - R, dim);
-            k0 = grid_axis(seed.z - R, dim);
-            nj = grid_axis(seed.y + R, dim) - j0 + 1;
-            nseg = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
-          } else {
-            nseg = 1;
+          if (lane == 0) {
+            if (exact) {
+              const int dim = PD(dim);
+              const float R =
+                  fminf(__fmaf_rn(PD(rt_max), 1.001f, Rc), __uint_as_float(reach_max_bits[pidx])) + 0.01f;
+              const int j0 = grid_axis(seed.y - R, dim), k0 = grid_axis(seed.z - R, dim);
+              const int nj = grid_axis(seed.y + R, dim) - j0 + 1;
+              S.scan[0] = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
+              S.scan[1] = nj;
+              S.scan[2] = grid_axis(seed.x - R, dim);
+              S.scan[3] = grid_axis(seed.x + R, dim);
+              S.scan[4] = j0;
+              S.scan[5] = k0;
+            } else {
+              S.scan[0] = 1;
+            }
           }
         }
         __syncwarp();
       }
       if (take) {
+        if (!COMPLETE && job == 2 && (S.site_flags & SITE_SECMISS)) {
+          // the largest |vertex - site|^2 of the site's pieces
+          float lm = 0.f;
+#pragma unroll
+          for (int k = 0; k < SL; ++k)
+            if (c.vm[k] & lane_bit) lm = fmaxf(lm, c.vw[k]);
+          lm = warp_max_nonneg(lm);
+          if (lane == 0) S.pr2 = fmaxf(S.pr2, lm);
+        }
         float vol, mx, my, mz;
         warp_moments(c, S.plane, lane, vol, mx, my, mz);
         if (lane == 0) {
-          V.add(vol);
-          MX.add(mx);
-          MY.add(my);
-          MZ.add(mz);
+          comp_add(S.acc[0], S.acc[4], vol);
+          comp_add(S.acc[1], S.acc[5], mx);
+          comp_add(S.acc[2], S.acc[6], my);
+          comp_add(S.acc[3], S.acc[7], mz);
           S.cnt[interior ? WC_INTERIOR : WC_CONTRIB]++;
           S.cnt[WC_FINAL] += (unsigned)c.nt;
         }
@@ -648,24 +879,44 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_clip_site(
       if (lane == 0) {
         out_list[atomicAdd(out_count, 1)] = s;
         S.cnt[WC_REDO]++;
+        if (CELL_TET && store.flags) store.flags[s] = (unsigned char)(S.site_flags | SITE_REDO);
       }
       __syncwarp();
       continue;
     }
-    if (lane == 0) mom[s] = make_dmom4(V.value(), MX.value(), MY.value(), MZ.value());
+    if (lane == 0) {
+      unsigned f = S.site_flags;
+      // a completion that failed keeps the earlier pass's moments
+      const bool keep_old = COMPLETE && (f & (SITE_UNRESOLVED | SITE_DROPPED));
+      if (!keep_old)
+        mom[s] = make_dmom4((double)S.acc[0] + (double)S.acc[4], (double)S.acc[1] + (double)S.acc[5],
+                            (double)S.acc[2] + (double)S.acc[6], (double)S.acc[3] + (double)S.acc[7]);
+      if (CELL_TET) {
+        if (!COMPLETE && exact && esc_list && (f & SITE_SECMISS)) {
+          // the cell is exact where it meets the mesh when its pieces lie
+          // within half the K-th neighbour's distance; else it is completed
+          // by the completion pass
+          const float4 seed = S.seed;
+          const float dK2 = dist2(seed, sites[knn[PD(knn_off) + (size_t)(s - PD(site_off)) * K + K - 1]]);
+          if (!(dK2 > __fmaf_rn(4.f * S.pr2, 1.0001f, 1e-4f))) {
+            const int pos = atomicAdd(esc_count, 1);
+            esc_list[pos] = s;
+            esc_r2[pos] = S.pr2;
+            f |= SITE_UNRESOLVED;
+          }
+        }
+        if (store.flags) store.flags[s] = (unsigned char)f;
+        if (!COMPLETE && (f & SITE_SECMISS)) {
+          S.cnt[WC_SECMISS]++;
+          if (prob_secmiss) atomicAdd(prob_secmiss + pidx, 1u);
+        }
+        if (COMPLETE) S.cnt[keep_old ? WC_UNRESOLVED : WC_COMPLETED]++;
+      }
+    }
     __syncwarp();
 #undef PD
   }
-  const unsigned cull_warp = __reduce_add_sync(FULL, cull_lane);
-  if (lane == 0) S.cnt[WC_CULLTESTS] += cull_warp;
-  __syncwarp();
-  if (stats && lane < WC_N) {
-    static const int slot[WC_N] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB,
-                                   STAT_SECURITY_MISS, STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES,
-                                   STAT_CLIPS, STAT_FINAL_VERTICES, STAT_CONFLICT_TESTS, STAT_CULL_TESTS,
-                                   STAT_NEW_VERTICES, STAT_INTERIOR, STAT_REDO, STAT_NEEDS_EXACT};
-    if (S.cnt[lane]) atomicAdd(stats + slot[lane], (unsigned long long)S.cnt[lane]);
-  }
+  if (stats && lane < WC_N && S.cnt[lane]) atomicAdd(stats + stat_slot(lane), (unsigned long long)S.cnt[lane]);
 }
 
 // Shared state of one lane group of k_build: its clip scratch; the group's
@@ -676,6 +927,7 @@ struct BuildSmem {
   unsigned conf[CAP];
   unsigned bedge[CAP];
   unsigned cnt[WC_N];
+  float4 seed;  // the group's site (read after the build rather than held in registers)
 };
 __host__ __device__ constexpr int build_plane_stride(int kmax) { return 4 + kmax + BOX_PLANES; }
 
@@ -689,7 +941,7 @@ __host__ __device__ constexpr int build_plane_stride(int kmax) { return 4 + kmax
 // counter independently; a warp's groups run one instruction stream, a
 // group whose cell is done passing its turn in each clip.
 template <bool BATCHED, int G, int SL, bool ROBUST>
-__global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_BUILD_MIN_BLOCKS) k_build(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
     unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,
@@ -718,7 +970,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     const int K = has ? PD(K) : 0;
     // with a tier, only the first K1 neighbour rows are computed yet
     const int K1 = (k_tier > 0 && k_tier < K) ? k_tier : K;
+    {
     const float4 seed = has ? sites[s] : make_float4(500.f, 500.f, 500.f, 0.f);
+    if (gl == 0) S.seed = seed;
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     if (has) {
       const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
@@ -738,7 +992,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
       const float sgn = (gl & 1) ? -1.f : 1.f;
       plane[4 + K + gl] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
     }
+    }
     __syncwarp();
+    const float L = plane[4 + K].w;  // the start cube's half side
     WarpCell<SL> c;
     cell_clear(c);
     if (has && gl < 8) {
@@ -763,7 +1019,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
       const float4 P = building ? plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
       if (building) seq_cnt += 1u + ((unsigned)c.nt << 16);
       const int r = group_clip<G, SL, ROBUST>(c, P, (unsigned)pi, plane, S.conf, S.bedge, gl, gbase, gid, building,
-                                              S.cnt + WC_EXACT);
+                                              S.cnt + WC_NEWV, S.cnt + WC_EXACT);
       if (building) {
         if (r == CLIP_EMPTY) {
           state = 1;
@@ -788,6 +1044,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
     // radius Rc, then the cell's vertex box against the summed table (the
     // test of k_clip_site)
     const bool built = has && state == 0 && !secmiss;
+    const float4 seed = S.seed;
     const float Rc = sqrtf(c.r2);
     const float Rq = __fmaf_rn(Rc, 1.001f, 0.01f);
     const int fdim = field ? PD(fdim) : 1;
@@ -861,6 +1118,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
       S.cnt[WC_PLANES] += seq_cnt & 0xffu;
       S.cnt[WC_CLIPS] += (seq_cnt >> 8) & 0xffu;
       S.cnt[WC_CONFLICT] += seq_cnt >> 16;
+      if (store.flags) store.flags[s] = interior ? SITE_INTERIOR : SITE_HANDED;
       if (!interior) {
         if (store.nt) store.nt[s] = keep ? (c.nt | (secmiss ? 256 : 0) | (deep ? (4 + K1) << 16 : 0)) : 0;
         out_list[atomicAdd(out_count, 1)] = s;
@@ -871,12 +1129,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
 #undef PD
   }
   if (stats) {
-    static const int slot[WC_N] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB,
-                                   STAT_SECURITY_MISS, STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES,
-                                   STAT_CLIPS, STAT_FINAL_VERTICES, STAT_CONFLICT_TESTS, STAT_CULL_TESTS,
-                                   STAT_NEW_VERTICES, STAT_INTERIOR, STAT_REDO, STAT_NEEDS_EXACT};
     for (int i = gl; i < WC_N; i += G)
-      if (S.cnt[i]) atomicAdd(stats + slot[i], (unsigned long long)S.cnt[i]);
+      if (S.cnt[i]) atomicAdd(stats + stat_slot(i), (unsigned long long)S.cnt[i]);
   }
 }
 
@@ -889,6 +1143,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, 8) k_build(
 constexpr int BUILD_G = 8, BUILD_SL = 4;
 static_assert(BUILD_G * BUILD_SL <= STORE_VERTS, "a stored cell holds a first-pass cell");
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
+// The completion pass (rare sites, often beside dense clusters: many faces)
+// runs with 256 vertices per cell.
+constexpr int SLOTS_COMPLETE = 8;
 
 template <class F>
 inline int resident_blocks(F kernel, int sms, int* out, size_t dyn_smem = 0) {
@@ -909,9 +1166,9 @@ inline size_t build_dyn_smem(int kmax) {
 template <bool R>
 struct ClipPasses {
   // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
-  // fast / redo, cell-tet batched fast / redo
+  // fast / redo, cell-tet batched fast / redo, completion lone / batched
   static int* resident() {
-    static int r[5] = {0, 0, 0, 0, 0};
+    static int r[7] = {0, 0, 0, 0, 0, 0, 0};
     return r;
   }
   static int prepare();
@@ -936,7 +1193,9 @@ int ClipPasses<R>::prepare() {
       resident_blocks(k_clip_site<true, false, SLOTS_FAST, R>, sms, r + 1) ||
       resident_blocks(k_clip_site<true, false, SLOTS_REDO, R>, sms, r + 2) ||
       resident_blocks(k_clip_site<true, true, SLOTS_FAST, R>, sms, r + 3) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_REDO, R>, sms, r + 4))
+      resident_blocks(k_clip_site<true, true, SLOTS_REDO, R>, sms, r + 4) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, sms, r + 5) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, sms, r + 6))
     return -2;
   return 0;
 }
@@ -985,30 +1244,35 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
     k_clip_site<false, false, SLOTS_TET_CELL, R><<<(int)(want < need ? want : need), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
         nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr,
-        CellStore{}, 0);
+        CellStore{}, 0, nullptr, nullptr, nullptr, nullptr);
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
   // counters: [0] sites the first pass hands on, [1] sites the one-warp pass
   // hands on, [2..4] the three passes' work counters, [5] the kNN's, [8] deep
   // sites (not done within the tier's neighbours), [9] their kNN's work
+  // counter, [10] sites to complete, [11] the completion pass's work
   // counter; lists: [0, n) the one-warp pass's hand-offs, [n, 2n) the first
-  // pass's, [2n, 3n) the deep sites
+  // pass's, [2n, 3n) the deep sites, [3n, 4n) the sites to complete and
+  // [4n, 5n) their pieces' squared radius bounds (float)
   const bool exact = tet_order != nullptr;
   int* const redo = lists;
   int* const rest = lists + n;
   int* const deep = lists + 2 * (size_t)n;
+  int* const esc = exact ? lists + 3 * (size_t)n : nullptr;
+  float* const esc_r2 = exact ? reinterpret_cast<float*>(lists + 4 * (size_t)n) : nullptr;
   const int kt = exact ? k_tier : 0;
-  VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 10 * sizeof(int), st));
+  VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 12 * sizeof(int), st));
   // every pass: one wave of resident blocks whose warps draw sites from a counter
   // the first pass's stored cells (exact form only)
-  const CellStore cs = exact ? store : CellStore{};
+  CellStore cs = store;
+  if (!exact) cs.tri = nullptr, cs.nt = nullptr;  // stored cells: exact form only
   auto launch = [&](auto kernel, int variant, const int* in_list, const int* in_count, int* out_list, int* out_count,
                     int* work) {
     kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
         tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, in_list, in_count, out_list,
-        out_count, work, cs, kt);
+        out_count, work, cs, kt, cell_start, esc, esc_r2, exact ? counters + 10 : nullptr);
   };
   if (exact) {
     if (kmax < 1 || kmax > MAX_SITE_K) {
@@ -1034,12 +1298,20 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
   }
   const int* in_list = exact ? rest : nullptr;
   const int* in_count = exact ? counters + 0 : nullptr;
+  // exact form: the sites whose cells their K neighbours left unresolved
+  // are completed last (128 vertices)
   if (probs) {
     launch(k_clip_site<true, true, SLOTS_FAST, R>, 3, in_list, in_count, redo, counters + 1, counters + 3);
     launch(k_clip_site<true, true, SLOTS_REDO, R>, 4, redo, counters + 1, nullptr, nullptr, counters + 4);
+    if (exact)
+      launch(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, 6, esc, counters + 10, nullptr, nullptr,
+             counters + 11);
   } else {
     launch(k_clip_site<true, false, SLOTS_FAST, R>, 1, in_list, in_count, redo, counters + 1, counters + 3);
     launch(k_clip_site<true, false, SLOTS_REDO, R>, 2, redo, counters + 1, nullptr, nullptr, counters + 4);
+    if (exact)
+      launch(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, 5, esc, counters + 10, nullptr, nullptr,
+             counters + 11);
   }
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;

@@ -185,11 +185,12 @@ __device__ __forceinline__ bool cavity_disk_small(int R, int nb) { return nb == 
 // computes the new vertex (the loop test: cavity_disk_small).  conf and
 // bedge are 32 SL-entry scratch arrays of
 // the warp.  need_r2: keep c.r2 (the largest |vertex|^2) current; callers that
-// never read it skip the warp reduction.
+// never read it skip the warp reduction.  nnew (shared, may be null): lane 0
+// adds the number of vertices a cut creates.
 template <int SL, bool ROBUST = false>
 __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
                                          unsigned* conf, unsigned* bedge, const int lane, const bool need_r2,
-                                         unsigned* nexact = nullptr) {
+                                         unsigned* nnew = nullptr, unsigned* nexact = nullptr) {
   const unsigned lane_bit = 1u << lane, lt_mask = lane_bit - 1u;
   unsigned m[SL];
   int nconf = 0;
@@ -320,6 +321,7 @@ __device__ __forceinline__ int warp_clip(WarpCell<SL>& c, const float4 P, const 
   // inconsistent (a plane through an edge, within rounding); drop the cell
   if (__any_sync(FULL, nonfinite)) return CLIP_BOUNDARY;
   c.nt = nt2;
+  if (nnew && lane == 0) *nnew += (unsigned)nb;
   if (need_r2) c.r2 = warp_max_nonneg(lm);
   __syncwarp();
   return CLIP_CUT;
@@ -472,11 +474,13 @@ __device__ __forceinline__ unsigned group_min_u(unsigned v, int gid) {
 // searches the group's removed triangles); each boundary vertex must start
 // and end exactly one boundary edge; the fan (pidx, a, b) fills freed slots.
 // Returns the group's result; the cell is changed only on CLIP_CUT.  conf and
-// bedge: the group's G SL-entry scratch arrays.
+// bedge: the group's G SL-entry scratch arrays; nnew (the group's, shared,
+// may be null): the group's lane 0 adds the vertices a cut creates.
 template <int G, int SL, bool ROBUST = false>
 __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
                                           unsigned* conf, unsigned* bedge, const int gl, const int gbase,
-                                          const int gid, const bool act, unsigned* nexact = nullptr) {
+                                          const int gid, const bool act, unsigned* nnew = nullptr,
+                                          unsigned* nexact = nullptr) {
   constexpr int CAP = G * SL;
   const unsigned lb = 1u << gl, ltm = lb - 1u;
   unsigned m[SL];
@@ -597,6 +601,7 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
     c.nt = nt2;
     c.r2 = r2;
     if (nf) res = CLIP_BOUNDARY;
+    if (nnew && gl == 0 && !nf) *nnew += (unsigned)nb;
   }
   __syncwarp();
   return res;

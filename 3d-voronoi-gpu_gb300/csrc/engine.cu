@@ -11,7 +11,8 @@
 //   cand       uint32[m][tk]         row-major (the reference keeps tk pitched rows)
 //   site_start int32[n + 1], site_fill int32[n], site_tets int32[m * tk]
 //   mom        dmom4[n]            volume, first moment
-//   stats      uint64[16]
+//   store      exact form: cells handed on by the first clip pass; site flags uint8[n]
+//   stats      uint64[VGB_STAT_COUNT]
 // One Lloyd iteration = grid sort -> kNN -> per-tet reach (exact form) or
 // candidates -> site-major lists (reference form) -> clip -> update, all on
 // one stream; with use_graph the iteration is captured once and replayed.
@@ -174,7 +175,7 @@ void free_engine(vgb_engine* e) {
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
                   e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph,
-                  e->redo_list, e->redo_count, e->store.tri, e->store.nt};
+                  e->redo_list, e->redo_count, e->store.tri, e->store.nt, e->store.flags};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -362,17 +363,19 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 3 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 12)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 5 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 12)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT)) ||
       (rc = dalloc(&e->store.tri, exact_form ? (size_t)n_site * STORE_VERTS : 1)) ||
-      (rc = dalloc(&e->store.nt, exact_form ? (size_t)n_site : 1))) {
+      (rc = dalloc(&e->store.nt, exact_form ? (size_t)n_site : 1)) ||
+      (rc = dalloc(&e->store.flags, cfg.method == VGB_METHOD_CELL_TET ? (size_t)n_site : 1))) {
     free_engine(e);
     return rc;
   }
   // neighbour rows start as valid indices (with the kNN in tiers a row's tail
   // is written only for the sites that need it)
   ce = cudaMemset(e->knn, 0, sizeof(unsigned) * (size_t)n_site * e->K);
+  if (ce == cudaSuccess) ce = cudaMemset(e->store.flags, 0, cfg.method == VGB_METHOD_CELL_TET ? (size_t)n_site : 1);
   if (ce != cudaSuccess) { set_error("memset: %s", cudaGetErrorString(ce)); free_engine(e); return VGB_ERR_CUDA; }
   for (auto& ev : e->ev) {
     ce = cudaEventCreate(&ev);
@@ -534,6 +537,7 @@ size_t vgb_engine_buffer_bytes(vgb_engine* e, int which) {
     case VGB_BUF_SITE_TETS:
       return e->cfg.method != VGB_METHOD_PLAIN && !e->field ? sizeof(int) * (size_t)e->n_tet * e->tk : 0;
     case VGB_BUF_MOMENTS: return sizeof(dmom4) * e->n;
+    case VGB_BUF_SITE_FLAGS: return e->cfg.method == VGB_METHOD_CELL_TET ? (size_t)e->n : 0;
   }
   return 0;
 }
@@ -551,6 +555,7 @@ int vgb_engine_copy_buffer(vgb_engine* e, int which, void* host, size_t bytes) {
     case VGB_BUF_SITE_START: src = e->site_start; break;
     case VGB_BUF_SITE_TETS: src = e->site_tets; break;
     case VGB_BUF_MOMENTS: src = e->mom; break;
+    case VGB_BUF_SITE_FLAGS: src = e->store.flags; break;
   }
   VGB_CUDA_TRY(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, e->st));
   VGB_CUDA_TRY(cudaStreamSynchronize(e->st));

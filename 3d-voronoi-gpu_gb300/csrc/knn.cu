@@ -28,6 +28,7 @@
 // the best 32*S keys (S slots per lane, held in registers).  After each shell
 // the buffer is flushed, and the walk stops once the k-th distance is below
 // the distance from the query to every cell beyond the shell.
+#include <atomic>
 #include <cfloat>
 
 #include "vgb_common.cuh"
@@ -166,8 +167,10 @@ __device__ __forceinline__ u64 kth_key(const u64 (&L)[S], int K) {
   return __shfl_sync(KFULL, v, (K - 1) & 31);
 }
 
+// Four resident CTAs per SM (32 warps): at that register budget (64 per
+// thread) the allocation spills nothing for S = 1, 2.
 template <int S, bool CENTROIDS>
-__global__ void __launch_bounds__(KNN_WARPS * 32) k_knn(const float4* __restrict__ sites,
+__global__ void __launch_bounds__(KNN_WARPS * 32, 4) k_knn(const float4* __restrict__ sites,
                                                         const int* __restrict__ cell_start,
                                                         const ProbDesc* __restrict__ probs,
                                                         const int* __restrict__ site_prob, ProbDesc lone,
@@ -347,15 +350,35 @@ __global__ void k_pos_of_id(const float4* __restrict__ sites, int n, const ProbD
   pos_of_id[P.site_off + site_id(sites[i])] = i;
 }
 
-static int g_knn_blocks = 0;  // resident CTAs (one wave), set by knn_prepare
+// Resident CTAs of the kNN kernel (one wave) per device, set by knn_prepare
+// with that device current.  Atomic: host threads driving different devices
+// may prepare and launch at the same time.
+constexpr int KNN_MAX_DEVICES = 64;
+static std::atomic<int> g_knn_blocks[KNN_MAX_DEVICES];
 
 int knn_prepare() {
   int dev = 0, sms = 0, per_sm = 0;
   VGB_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= KNN_MAX_DEVICES) {
+    set_error("kNN: device %d beyond the supported %d", dev, KNN_MAX_DEVICES);
+    return -1;
+  }
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn<2, false>, KNN_WARPS * 32, 0));
-  g_knn_blocks = sms * (per_sm > 0 ? per_sm : 1);
+  g_knn_blocks[dev].store(sms * (per_sm > 0 ? per_sm : 1));
   return 0;
+}
+
+// The current device's resident kNN CTAs (prepared on first use); 0 on error.
+static int knn_blocks() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= KNN_MAX_DEVICES) {
+    set_error("kNN: no usable current device");
+    return 0;
+  }
+  int b = g_knn_blocks[dev].load();
+  if (b == 0 && knn_prepare() == 0) b = g_knn_blocks[dev].load();
+  return b;
 }
 
 template <bool CENTROIDS>
@@ -367,9 +390,10 @@ static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc
     set_error("kNN: k=%d outside [1, 128]", kmax);
     return -1;
   }
-  if (g_knn_blocks == 0 && knn_prepare()) return -1;
+  const int resident = knn_blocks();
+  if (resident <= 0) return -1;
   const int need = (n_query + KNN_WARPS - 1) / KNN_WARPS;
-  const int want = work ? g_knn_blocks : 8 * g_knn_blocks;  // round-robin: eight waves
+  const int want = work ? resident : 8 * resident;  // round-robin: eight waves
   const int blocks = need < want ? need : want;
   if (work) VGB_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   if (kmax <= 32)

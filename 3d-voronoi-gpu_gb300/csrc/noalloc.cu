@@ -13,8 +13,13 @@
 //
 // Host code never dereferences the array's name: on the host it is only a
 // stand-in, not a device address.  The first call on each device (with that
-// device current) looks the address up with cudaGetSymbolAddress and sets the
-// kNN kernel's shared-memory limit; later calls reuse both.
+// device current) looks the array's device address up with
+// cudaGetSymbolAddress and records the kNN kernel's resident block count for
+// that device (an occupancy query); later calls on the device reuse both.
+// That first call should therefore come before any stream capture.  Every
+// call shares the one array and leaves its contents behind (each call clears
+// the counters it needs), so calls that overlap on the GPU -- two streams, or
+// two host threads on one device -- race on it.
 #include <cuda_runtime.h>
 
 #include <mutex>

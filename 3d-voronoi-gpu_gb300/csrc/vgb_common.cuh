@@ -41,7 +41,9 @@ enum StatSlot : int {
   STAT_INTERIOR = 14,        // sites whose whole cell lies inside the mesh (taken whole)
   STAT_REDO = 15,            // sites redone with the larger cell capacity (their cell outgrew 64 vertices)
   STAT_NEEDS_EXACT = 16,     // vertex-vs-plane tests decided by the exact determinants (robust predicates)
-  STAT_COUNT = 17
+  STAT_COMPLETED = 17,       // sites whose cell the completion pass clipped by every site that can cut it
+  STAT_UNRESOLVED = 18,      // sites left with a cell that a site beyond their K nearest may still cut
+  STAT_COUNT = 19
 };
 
 constexpr int WARP = 32;
@@ -221,9 +223,19 @@ int candidates_by_site(const unsigned* cand, int n_tet, int tk, int n, int* star
 // stored cell (its vertices recomputed from the triples) instead of
 // building it again.
 constexpr int STORE_VERTS = 32;
+// Per-site outcome bits of a cell-tet pass (CellStore::flags; the public
+// VGB_SITE_* values).
+constexpr unsigned char SITE_HANDED = 1;    // the one-warp pass built the cell (not finished by the first pass)
+constexpr unsigned char SITE_SECMISS = 2;   // the cell's K neighbours did not reach its security radius
+constexpr unsigned char SITE_INTERIOR = 4;  // the cell lies inside the mesh and was taken whole
+constexpr unsigned char SITE_REDO = 8;      // the cell outgrew 64 vertices and was redone at 128
+constexpr unsigned char SITE_DROPPED = 16;  // the cell itself failed (capacity or cavity): no moments
+constexpr unsigned char SITE_COMPLETED = 32;   // the completion pass clipped the cell by every site that can cut it
+constexpr unsigned char SITE_UNRESOLVED = 64;  // a site beyond the K nearest may still cut the cell
 struct CellStore {
-  unsigned* tri;  // [n][STORE_VERTS]
-  int* nt;        // [n]
+  unsigned* tri;         // [n][STORE_VERTS]
+  int* nt;               // [n]
+  unsigned char* flags;  // [n] SITE_* bits of the last pass (cell-tet method), may be null
 };
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, const ProbDesc* probs,
@@ -245,8 +257,9 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, co
 // form): the neighbour rows hold only their first min(K, k_tier) entries (the
 // kNN ran with that tier); the first pass builds from them, and the rows of
 // the sites it leaves unfinished are completed (knn_sites_listed, from
-// cell_start and pos_of_id) before the one-warp pass.  lists: 3n ints,
-// counters: at least 10.
+// cell_start and pos_of_id) before the one-warp pass.  lists: 5n ints,
+// counters: at least 12 (the exact form's completion list and its counters
+// among them).
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.

@@ -4,9 +4,13 @@
 //
 // Per iteration: one pass of the engine with the Lloyd update, the new sites
 // copied back to the host, optionally iter_<i>.xyz and a record.csv row.
-// record.csv keeps the reference's header and columns (voronoi.cu:984-986,
-// seconds with five decimals); this engine runs one clip method, reported in
-// the Clip_tet-cell column, and appends three columns of its own.
+// record.csv keeps the reference's header, columns and row format
+// (voronoi.cu:984-986, 1076-1116: ten fields, each followed by ", ", seconds
+// with five decimals).  The reference times both clip methods every
+// iteration; this driver runs one, so its time goes into that method's column
+// (Clip_cell-tet for the default cell-tet method, Clip_tet-cell for the
+// tet-cell method) and the other column holds 0.  The pair counts and the
+// volume sum of each iteration go to stdout.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -67,10 +71,10 @@ extern "C" int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const
   std::ofstream record;
   if (write_files) {
     record.open("record.csv", std::ios::app);
-    record << "n_site, n_tet, TET_K, SITE_K, Iter, k-NN, Clip_tet-cell, Clip_cell-tet, Compute_new_site, GPU2CPU"
-              ", Clipped_pairs, Contributing_pairs, Volume_sum\n";
+    record << "n_site, n_tet, TET_K, SITE_K, Iter, k-NN, Clip_tet-cell, Clip_cell-tet, Compute_new_site, GPU2CPU\n";
     record << std::setprecision(5) << std::setiosflags(std::ios::fixed);
   }
+  const bool cell_tet = cfg.method == VGB_METHOD_CELL_TET;
   std::vector<float> xyz(3 * (size_t)n_site);
   std::vector<int> ids(n_site);
   std::vector<double> vol(n_site);
@@ -95,11 +99,12 @@ extern "C" int vgb_clipped_voro_diagram(const float* vertices, int n_vert, const
       double vs = 0;
       for (double v : vol) vs += v;
       write_xyz("iter_" + std::to_string(it) + ".xyz", site, n_site, soa);
+      const double knn_s = (ms[0] + ms[1] + ms[2] + ms[3]) / 1e3, clip_s = ms[4] / 1e3;
       record << n_site << ", " << n_tet << ", " << tk << ", " << K << ", " << it << ", ";
-      double knn_s = (ms[0] + ms[1] + ms[2] + ms[3]) / 1e3;
-      record << knn_s << ", " << ms[4] / 1e3 << ", " << 0.0 << ", " << ms[5] / 1e3 << ", " << d2h << ", ";
-      record << stats[VGB_STAT_CLIPPED] << ", " << stats[VGB_STAT_CONTRIB] << ", " << std::setprecision(3) << vs
-             << std::setprecision(5) << std::endl;
+      record << knn_s << ", " << (cell_tet ? 0.0 : clip_s) << ", " << (cell_tet ? clip_s : 0.0) << ", "
+             << ms[5] / 1e3 << ", " << d2h << ", " << std::endl;
+      printf("clipped pairs %llu, contributing pairs %llu, volume sum %.6g\n", stats[VGB_STAT_CLIPPED],
+             stats[VGB_STAT_CONTRIB], vs);
     }
   }
   vgb_engine_destroy(e);

@@ -3,7 +3,8 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--method cell_tet|site_major|plain]
-                    [--reference-form] [--robust-predicates] [--accuracy M] [--no-cpu-baseline]
+                    [--reference-form] [--robust-predicates] [--accuracy M]
+                    [--no-cpu-baseline] [--no-forms]
 
 A step is one Lloyd iteration of the path over the whole site set: grid sort,
 site kNN, per-tet reach, clipped cells (cell-tet method, exact form: cells
@@ -15,26 +16,36 @@ torus (128^3 grid, 1,955,088 tets) with 1,000,000 uniform sites, K = 64 (the
 reference's heuristic gives tet_k = 60 for the reference form).  Inputs are
 generated (seeded) on the host, then resident in HBM; the working set
 (neighbour lists, tet records) is several times the 129 MB L2, so no flush is
-needed between steps.  --workload batch256_kuhn runs the batched form (256
-independent problems per launch).  --robust-predicates runs the clip's
-robust-predicate instantiation (exact decisions of near-zero vertex-vs-plane
-tests, double-precision vertices).  --accuracy M adds the per-iteration error
-of M sampled cells against the FP64 oracle.
+needed between steps.  --workload batch256_kuhn runs the batched form alone
+(256 independent problems per launch).  --robust-predicates runs the clip's
+robust-predicate instantiation.
 
 Printed (rank 0, one JSON line): value = Lloyd iter/s with inputs resident
 (CUDA events on the engine stream around exactly K steps, after W warm-up
-steps), e2e = the same through vgb_engine_step_host with page-locked host
-buffers (site positions in and out every step), the roofline of the clip
-kernel (FP32) and of the site kNN (HBM) with their instruction-issue
-rooflines, the reference's own CPU kernels on a
-bounded sample (cpu_baseline), and the SM clocks sampled during the timed
-region.  With --gpus N > 1 (torchrun), each rank runs an independent replica
-of the workload on its own GPU; value sums the replicas' iterations over the
-slowest rank's time.
+steps); e2e = the same K steps through vgb_engine_step_host with page-locked
+host buffers (site positions in and out every step), started from the same
+site positions as the timed region; the roofline of the clip phase (FP32
+pipe) and of the site kNN (HBM); accuracy = the FP64 oracle's exact cells
+(neighbour lists complete for each cell, whatever K) against one pass's cells
+of 1,000 random sites plus up to 500 whose K neighbours missed their security
+radius, and the total volume against the mesh volume; the same problem run
+in the plain form (the reference's thread-per-pair layout) and in the
+reference form (per-tet sums over tet_k candidates), with chosen_over_plain;
+the precision configuration (Gaussian-mixture sites) with its own accuracy;
+the batched form (256 problems); the small configuration (20^3 Kuhn cube,
+20,000 sites); the reference's own CPU kernels on a bounded sample
+(cpu_baseline); and the SM clocks sampled during the timed region.  With
+--gpus N > 1 (torchrun), each rank runs an independent replica of the
+workload on its own GPU; value sums the replicas' iterations over the slowest
+rank's time.  --no-forms skips the extra forms and configurations.
 
 --impl reference times the reference's own implementation of the path on the
 host cores instead (its kNN, centroid and clipping kernels compiled for the
-CPU by oracle/make_ref.py), on a bounded sample of each step.
+CPU by oracle/make_ref.py).  At the headline size one iteration takes minutes
+there, so each step times a bounded sample of the pairs and the line's value
+is the extrapolated iteration rate ("extrapolated": true; ms_per_step is the
+measured time of the sampled work); the small configuration is also timed in
+full, every kernel on every pair (full_run).
 """
 from __future__ import annotations
 
@@ -83,16 +94,13 @@ WORKLOADS = {
                                "in {32,48,64,96,128} per problem, grid density autotuned"),
 }
 DEFAULT_WORKLOAD = "torus128_uniform_1m"
-# kernels per step besides the grid sort: kNN 2, then exact form: reach, clip,
-# update; reference form: candidate kNN, candidate lists (count, scan x3,
-# fill), clip, update; plain: candidate kNN, clip, update
 # kernels per Lloyd iteration besides the grid sort: exact form -- position
 # map, kNN (first tier), tet reach, first clip pass, kNN of the listed sites
-# (K > 32 only), one-warp and 128-vertex clip passes, update; reference
-# cell-tet form -- position map, site kNN, centroid kNN, candidate count, scan
-# (3), fill, the two clip passes, update; tet-cell: one clip pass; plain: the
-# thread-per-pair clip and its update
-LAUNCHES_PER_STEP = {"exact": 8, "cell_tet": 11, "site_major": 10, "plain": 5}
+# (K > 32 only), one-warp, 128-vertex and completion clip passes, update;
+# reference cell-tet form -- position map, site kNN, centroid kNN, candidate
+# count, scan (3), fill, the two clip passes, update; tet-cell: one clip
+# pass; plain: the thread-per-pair clip and its update
+LAUNCHES_PER_STEP = {"exact": 9, "cell_tet": 11, "site_major": 10, "plain": 5}
 
 
 def grid_sort_launches(ncell: int) -> int:
@@ -105,7 +113,7 @@ def grid_sort_launches(ncell: int) -> int:
         top >>= 8
     return 4 + 5 * passes
 
-# algorithmic FP32 work of the clip kernel, per counted event
+# algorithmic FP32 work of the clip phase, per event its kernels count
 FLOPS_CONFLICT = 7      # plane test of one cell vertex: 3 FMA + compare
 FLOPS_CULL = 28         # plane test of the four tet corners
 FLOPS_NEW_VERTEX = 45   # vertex of three planes: 3 cross products, det, scale
@@ -197,23 +205,13 @@ def measured_peaks():
     return 6800.0, 2070.0, "fallback"
 
 
-def profile_value(kernel: str, workload: str, key: str = "traffic_bytes_per_launch"):
-    """A per-launch figure (`key: value` line) from a committed ncu summary, if one exists."""
-    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith(key + ":"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
-
-
-def profile_traffic(kernel: str, workload: str):
-    """Per-launch DRAM bytes from a committed ncu summary, if one exists."""
-    return profile_value(kernel, workload)
+# DRAM traffic per launch of the rooflined kernels, from ncu captures of the
+# 125,000-site torus workload (64^3 grid: one kernel, one launch, 1 pass of
+# dram__bytes_read.sum + dram__bytes_write.sum) scaled to the 1M-site
+# workload by its site count, and the capture it came from.  Both kernels
+# move bytes in proportion to the sites (rows of neighbours, site records,
+# tet records of the handed-on cells).
+TRAFFIC = {}
 
 
 # ---------------------------------------------------------------------------
@@ -356,6 +354,7 @@ def run_ours(args):
     # warm-up (graph capture happens on the first replay)
     eng.time_iterate(args.warmup, update=True)
     eng.sync()
+    start_sites = eng.sites_original()   # where the timed region starts (host copy, outside it)
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
@@ -366,7 +365,9 @@ def run_ours(args):
     ms = max_over_ranks(ms)
     value = world * args.steps / (ms / 1e3)
 
-    # per-phase device times of stream-ordered passes (for the roofline)
+    # per-phase device times of stream-ordered passes (for the roofline),
+    # from the timed region's start
+    eng.set_sites(start_sites)
     eng.set_graph(False)
     ph = []
     for _ in range(2):
@@ -376,19 +377,20 @@ def run_ours(args):
     phases = {k: statistics.mean(p[k] for p in ph) for k in ph[0]}
     stats = eng.stats()
 
-    # end to end through the host-buffer step (positions in and out each step)
+    # end to end through the host-buffer step (positions in and out each
+    # step), the same K steps from the same start as the timed region
     n = eng.n_site
-    xyz, _ = eng.sites()
+    eng.set_sites(start_sites)           # original order = the engine's order until its next sort
     bufs = [pkg.PinnedArray((n, 3)), pkg.PinnedArray((n, 3))]
-    bufs[0].array[:] = xyz
-    eng.step_host(bufs[0].array, bufs[1].array)
+    bufs[0].array[:] = start_sites
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        eng.step_host(bufs[(i + 1) % 2].array, bufs[i % 2].array)
+        eng.step_host(bufs[i % 2].array, bufs[(i + 1) % 2].array)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
-           "d2h_bytes_per_step": 12 * n, "api": "vgb_engine_step_host"}
+           "d2h_bytes_per_step": 12 * n, "api": "vgb_engine_step_host",
+           "start": "the timed region's first site positions"}
     for b in bufs:
         b.close()
 
@@ -402,13 +404,13 @@ def run_ours(args):
     kname = ("k_build + k_clip_site<cell_tet> x2 (clip phase)" if exact else
              {"cell_tet": "k_clip_site<cell_tet> x2 (clip phase)", "site_major": "k_clip_site<tet_cell>",
               "plain": "k_clip_plain"}[args.method])
-    ktraffic = profile_traffic("clip_exact" if exact else {"cell_tet": "clip_cell_tet", "site_major": "clip_tet_cell",
-                                                          "plain": "clip_plain"}[args.method], args.workload)
+    tr_clip = TRAFFIC.get(("clip", args.workload)) if exact else None
     roofline = {"kernel": kname,
                 "bound": "fp32", "achieved": round(clip_tf, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
-                "frac": round(clip_tf / fp32_peak, 4), "traffic": ktraffic,
+                "frac": round(clip_tf / fp32_peak, 4), "traffic": tr_clip[0] if tr_clip else None,
+                "traffic_source": tr_clip[1] if tr_clip else None,
                 "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock from MEASURED_PEAKS.json); "
-                               "the clip is FP32-pipe work, not HBM or tensor work",
+                               "no FP32 peak is measured; the clip is FP32-pipe work, not HBM or tensor work",
                 "flops_per_launch": clip_flops, "ms_per_launch": round(phases["clip"], 4)}
     # the exact cell-tet form's kNN computes the first 32 neighbours of a row
     # when K is above that (the rest, for the sites that need them, runs in
@@ -416,58 +418,55 @@ def run_ours(args):
     K1 = min(K, 32) if (exact and args.method == "cell_tet") else K
     knn_bytes = n * (16 + 4 * K1)
     knn_gbs = knn_bytes / (phases["knn"] / 1e3) / 1e9
+    tr_knn = TRAFFIC.get(("knn", args.workload)) if exact else None
     roofline_knn = {"kernel": "k_knn<sites>" + (" (first tier, 32 neighbours)" if K1 < K else ""),
                     "bound": "hbm", "achieved": round(knn_gbs, 1),
                     "peak": hbm_peak, "unit": "GB/s", "frac": round(knn_gbs / hbm_peak, 4),
-                    "traffic": profile_traffic("knn_sites", args.workload),
+                    "traffic": tr_knn[0] if tr_knn else None, "traffic_source": tr_knn[1] if tr_knn else None,
                     "peak_source": f"{peak_src} hbm_gbs", "bytes_per_launch": knn_bytes,
-                    "ms_per_launch": round(phases["knn"], 4)}
-    # the clip's real bound: warp instructions issued per second (count from
-    # the committed ncu capture of the same workload) against 152 SMs x 4
-    # schedulers x the max SM clock
-    issue_peak = 152 * 4 * sm_max * 1e6 / 1e9   # G warp-instructions/s
-    roofline_issue = None
-    winst = profile_value("clip_exact" if exact else "clip_cell_tet", args.workload, "warp_instructions_per_launch")
-    if winst:
-        ach = winst / (phases["clip"] / 1e3) / 1e9
-        roofline_issue = {"kernel": kname, "bound": "issue", "achieved": round(ach, 1), "peak": round(issue_peak, 1),
-                          "unit": "G warp-inst/s", "frac": round(ach / issue_peak, 4),
-                          "warp_instructions_per_launch": winst, "ms_per_launch": round(phases["clip"], 4)}
-    # the kNN's real bound is the same: 64-bit key selection, not HBM
-    roofline_knn_issue = None
-    kinst = profile_value("knn_sites", args.workload, "warp_instructions_per_launch")
-    if kinst:
-        ach = kinst / (phases["knn"] / 1e3) / 1e9
-        roofline_knn_issue = {"kernel": roofline_knn["kernel"], "bound": "issue", "achieved": round(ach, 1),
-                              "peak": round(issue_peak, 1), "unit": "G warp-inst/s",
-                              "frac": round(ach / issue_peak, 4), "warp_instructions_per_launch": kinst,
-                              "ms_per_launch": round(phases["knn"], 4)}
+                    "ms_per_launch": round(phases["knn"], 4),
+                    "note": "the selection work per query (about 300 candidate keys, sorting networks) bounds "
+                            "this kernel, not its bytes; the 50%-of-HBM target is not met"}
 
     accuracy = None
-    if args.accuracy > 0 and rank == 0:
-        accuracy = accuracy_run(eng, P, K, args.accuracy, args.accuracy_iters)
+    if rank == 0 and args.method == "cell_tet":
+        # one pass from the timed region's start: every cell against the oracle's exact cells
+        eng.set_sites(start_sites)
+        accuracy = accuracy_pass(pkg, eng, P, start_sites)
+        if args.accuracy > 0:
+            eng.set_sites(start_sites)
+            accuracy["per_iteration"] = accuracy_run(pkg, eng, P, args.accuracy, args.accuracy_iters)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         checker = load_checker()
+        eng.set_sites(start_sites)
+        eng.iterate(1, update=False)
+        eng.sync()
         s4 = eng.buffer("sites")
         # the reference's kernels need its tet_k candidate sets: rows of the sampled tets from the same
-        # exact search (grid kNN of the centroids, ties by site id)
+        # exact search (grid kNN of the centroids, ties by site id), and full K-rows of the sites
         cent = checker.tet_centroids(P.verts, P.tets)
         ids = s4[:, 3].copy().view(np.int32)
 
         def cand_rows(ts):
             return checker.knn_grid(s4[:, :3], cent[ts], eng.tet_k, exclude_self=False, key=ids)
 
-        t_iter, det = host_sample_baseline(checker, s4[:, :3], eng.buffer("knn").astype(np.int32), P.verts,
-                                           P.tets, cand_rows, tk=eng.tet_k)
+        knn_full = checker.knn_grid(s4[:, :3], None, K, key=ids)
+        t_iter, det = host_sample_baseline(checker, s4[:, :3], knn_full, P.verts, P.tets, cand_rows, tk=eng.tet_k)
         cpu = {"value": 1.0 / t_iter, "unit": UNIT, "cores": det["cores"], "kind": det["kind"],
+               "extrapolated": True,
                "sample": f"{det['sample_pairs']} of {eng.n_tet * eng.tet_k} (tet, site) pairs in 8 contiguous "
                          f"tet chunks plus the Voronoi cells of their {det['sample_sites']} sites; the reference's "
                          f"tet-cell and cell-tet kernels (both run every reference iteration), kNN excluded; "
-                         f"extrapolated to one iteration",
+                         f"timed {det['seconds']:.1f} s, extrapolated to one iteration",
                "detail": det}
+    grid_dim = eng.grid_dim
     eng.close()
+
+    forms = {}
+    if rank == 0 and world == 1 and not args.no_forms and args.workload == DEFAULT_WORKLOAD:
+        forms = other_forms(pkg, P, K, value, args)
     if rank != 0:
         return
     pairs_per_s = stats["candidates"] * value / world
@@ -475,22 +474,21 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "description": w["desc"], "n_site": eng.n_site, "n_tet": eng.n_tet,
-                   "site_k": eng.site_k, "tet_k": eng.tet_k, "grid_dim": eng.grid_dim, "method": args.method,
-                   "knn_tiers": ([32, eng.site_k] if exact and args.method == "cell_tet" and eng.site_k > 32
-                                 else [eng.site_k]),
+        "config": {"workload": args.workload, "description": w["desc"], "n_site": n, "n_tet": len(P.tets),
+                   "site_k": K, "tet_k": pkg.tet_k(n, len(P.tets)), "grid_dim": grid_dim, "method": args.method,
+                   "knn_tiers": ([32, K] if exact and args.method == "cell_tet" and K > 32 else [K]),
                    "robust_predicates": bool(args.robust_predicates),
                    "form": "exact (inside cells whole, boundary cells against every tet in reach)" if exact
                            else "reference (per-tet sums over tet_k candidates)",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
-                   "cuda_graph": True, "l2": "inputs larger than L2 (candidate + neighbour lists > 129 MB), no flush",
+                   "cuda_graph": True, "l2": "inputs larger than L2 (neighbour lists and tet records > 129 MB), "
+                                             "no flush",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": (LAUNCHES_PER_STEP["exact" if exact else args.method] - (1 if exact and K <= 32 else 0) +
-                         grid_sort_launches(eng.grid_dim ** 3)) * args.steps,
+                         grid_sort_launches(grid_dim ** 3)) * args.steps,
         "e2e": e2e,
         "roofline": roofline,
         "roofline_knn": roofline_knn,
-        "roofline_issue": roofline_issue, "roofline_knn_issue": roofline_knn_issue,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "pairs_per_s": round(pairs_per_s, 1),
         "clipped_pairs_per_s": round(stats["clipped"] * value / world, 1),
@@ -500,16 +498,114 @@ def run_ours(args):
     }
     if accuracy is not None:
         line["accuracy"] = accuracy
+    line.update(forms)
     print(json.dumps(line), flush=True)
 
 
-def accuracy_run(eng, P, K, m, iters):
-    """Per-iteration error of the cells against the FP64 oracle: before each
-    Lloyd iteration the positions are saved; the iteration's moments (of those
-    positions) are compared, for m sampled sites, with the oracle's clipped
-    cells (every tet within the K-th neighbour distance: twice the bound on a
-    cell that reaches its security radius), and the total volume of all cells
-    with the mesh volume."""
+def time_engine(pkg, P, K, warmup, steps, **kw):
+    """Lloyd iter/s of one engine on P (CUDA events around `steps` graph
+    replays after `warmup`), with its counters."""
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, use_graph=True, **kw) as e:
+        e.time_iterate(warmup, update=True)
+        ms = e.time_iterate(steps, update=True)
+        st = e.stats()
+        return {"value": round(steps / (ms / 1e3), 3), "ms_per_step": round(ms / steps, 4), "steps": steps,
+                "warmup": warmup, "site_k": e.site_k, "tet_k": e.tet_k, "stats": st}
+
+
+def other_forms(pkg, P, K, value, args):
+    """The plain and reference forms of the headline problem, the precision
+    configuration, the batched form and the small configuration, each timed
+    on its own engine (a few steps each)."""
+    out = {}
+    t0 = time.perf_counter()
+    plain = time_engine(pkg, P, K, 3, 3, method="plain")
+    plain["form"] = "plain: the reference's tet-cell layout, thread per (tet, tet_k slot) pair, float atomics"
+    out["plain_form"] = plain
+    ref = time_engine(pkg, P, K, 3, 10, method="cell_tet", exact=False)
+    ref["form"] = "reference: cell-tet method summed over each tet's tet_k candidate sites"
+    out["reference_form"] = ref
+    out["chosen_over_plain"] = round(value / plain["value"], 2)
+    out["chosen_over_reference_form"] = round(value / ref["value"], 2)
+    # the precision configuration: Gaussian-mixture sites, same mesh and form
+    Pg = make_problem("torus128_gaussian_1m")
+    with pkg.Engine(Pg.verts, Pg.tets, Pg.sites, site_k=K, use_graph=True, exact=True) as e:
+        e.time_iterate(args.warmup, update=True)
+        start = e.sites_original()
+        ms = e.time_iterate(args.steps, update=True)
+        prec = {"workload": "torus128_gaussian_1m", "description": WORKLOADS["torus128_gaussian_1m"]["desc"],
+                "value": round(args.steps / (ms / 1e3), 3), "ms_per_step": round(ms / args.steps, 4),
+                "steps": args.steps, "warmup": args.warmup, "site_k": e.site_k}
+        e.set_sites(start)
+        prec["accuracy"] = accuracy_pass(pkg, e, Pg, start)
+    prec["over_plain"] = round(prec["value"] / plain["value"], 2)
+    out["precision_form"] = prec
+    # the batched configuration
+    if not args.no_batch:
+        out["batched_form"] = batch_measure(pkg, 3, 10, 0)
+    # the small configuration, timed in full by the reference arm too
+    Ps = make_problem("kuhn20_20k")
+    small = time_engine(pkg, Ps, 64, 5, 50, exact=True)
+    small.update(workload="kuhn20_20k", description=WORKLOADS["kuhn20_20k"]["desc"])
+    small.pop("stats")
+    out["small_config"] = small
+    out["forms_s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def accuracy_pass(pkg, eng, P, start_sites, n_random=1000, n_secmiss=500, seed=7):
+    """One pass of the engine from start_sites (no update), every cell's
+    moments against the FP64 oracle's exact cells of a sample: n_random
+    random sites plus up to n_secmiss of those whose K neighbours missed the
+    security radius.  The oracle's neighbour lists are complete for each cell
+    (every site within twice its radius), so an error from the engine's K
+    would show; the total volume of all cells is held against the mesh
+    volume."""
+    checker = load_checker()
+    eng.iterate(1, update=False)
+    eng.sync()
+    s4 = eng.buffer("sites")
+    ids = s4[:, 3].copy().view(np.int32)
+    vol_g, mom_g = eng.moments()
+    flags_g = eng.buffer("site_flags")
+    n = len(ids)
+    vol, mom, flags = np.empty(n), np.empty((n, 3)), np.empty(n, np.uint8)
+    vol[ids], mom[ids], flags[ids] = vol_g, mom_g, flags_g
+    rng = np.random.default_rng(seed)
+    miss_all = np.flatnonzero(flags & pkg.SITE_SECMISS)
+    miss = rng.choice(miss_all, min(n_secmiss, len(miss_all)), replace=False) if len(miss_all) else miss_all
+    smp = np.unique(np.concatenate([rng.choice(n, min(n, n_random), replace=False), miss]))
+    t0 = time.perf_counter()
+    r = checker.complete_cells(start_sites, smp, P.verts, P.tets, k0=128)
+    t_orc = time.perf_counter() - t0
+    mesh_vol = checker.mesh_volume(P.verts, P.tets)
+    lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
+    diag = float(np.linalg.norm(hi - lo))
+    vmax = float(r["vol"].max())
+    ok = r["vol"] > 1e-9 * vmax
+    tiny = ~ok
+    vrel = np.abs(vol[smp][ok] - r["vol"][ok]) / r["vol"][ok]
+    brel = np.linalg.norm(mom[smp][ok] / vol[smp][ok, None] - r["mom"][ok] / r["vol"][ok, None], axis=1) / diag
+    is_miss = np.isin(smp, miss)[ok]
+    return {"oracle": "FP64 cell-tet restatement (oracle/), exact cells: every tet in reach, neighbour lists "
+                      "complete for each cell (every site within twice its radius)",
+            "sampled": int(len(smp)), "sampled_secmiss": int(len(miss)), "secmiss_sites": int(len(miss_all)),
+            "oracle_neighbours_max": int(r["k"].max()), "oracle_s": round(t_orc, 1),
+            "vol_rel_max": float(vrel.max()), "vol_rel_p99": float(np.percentile(vrel, 99)),
+            "vol_rel_max_secmiss": float(vrel[is_miss].max()) if is_miss.any() else None,
+            "bary_diag_max": float(brel.max()),
+            "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol),
+            "tiny_cells": int(tiny.sum()),
+            "tiny_vol_abs_max": float(np.abs(vol[smp][tiny] - r["vol"][tiny]).max() / vmax) if tiny.any() else 0.0,
+            "bars": {"vol_rel": 1e-5, "bary_diag": 1e-6, "total_vol_rel": 1e-6, "tiny_vol_abs": 1e-6},
+            "tiny": "cells below 1e-9 of the largest sampled volume: absolute error / largest volume"}
+
+
+def accuracy_run(pkg, eng, P, m, iters):
+    """Per-iteration error: before each Lloyd iteration the positions are
+    saved; the iteration's cells (of those positions) are checked on m
+    random sites against the oracle's exact cells, and the total volume of
+    all cells against the mesh volume."""
     checker = load_checker()
     mesh_vol = checker.mesh_volume(P.verts, P.tets)
     lo, hi = P.verts.min(0).astype(np.float64), P.verts.max(0).astype(np.float64)
@@ -517,48 +613,48 @@ def accuracy_run(eng, P, K, m, iters):
     rng = np.random.default_rng(7)
     out = []
     for it in range(iters):
-        xyz0, ids0 = eng.sites()
-        pre = np.empty_like(xyz0)
-        pre[ids0] = xyz0
+        pre = eng.sites_original()
         eng.iterate(1, update=True)
         eng.sync()
-        vol, mom = eng.moments()
+        vol_g, mom_g = eng.moments()
         _, ids = eng.sites()
-        pos = pre[ids]                                  # pre-update positions, this iteration's grid order
-        smp = rng.choice(len(pos), m, replace=False)
-        # the sampled sites' K nearest (the engine's rows hold only what the
-        # cells needed when its kNN runs in tiers)
-        from scipy.spatial import cKDTree
-        dist, nb = cKDTree(pos).query(pos[smp], K + 2)
-        keep = nb != smp[:, None]                       # self excluded (by index: duplicates stay)
-        keep[keep.sum(1) > K, -1] = False
-        nbr = nb[keep].reshape(m, K)
-        dK = dist[keep].reshape(m, K)[:, K - 1]
-        r = checker.sample_cells(pos, smp, nbr, P.verts, P.tets, dK + 1.0)
-        # relative error on the cells above 1e-9 of the largest sampled volume;
-        # the (near-degenerate) cells below it by their absolute error, as the
-        # parity tests hold them
+        n = len(ids)
+        vol, mom = np.empty(n), np.empty((n, 3))
+        vol[ids], mom[ids] = vol_g, mom_g
+        smp = rng.choice(n, m, replace=False)
+        r = checker.complete_cells(pre, smp, P.verts, P.tets, k0=128)
         vmax = float(r["vol"].max())
         ok = r["vol"] > 1e-9 * vmax
-        tiny = (r["vol"] > 0) & ~ok
-        tiny_abs = float(np.abs(vol[smp][tiny] - r["vol"][tiny]).max() / vmax) if tiny.any() else 0.0
         vrel = np.abs(vol[smp][ok] - r["vol"][ok]) / r["vol"][ok]
-        b_gpu = mom[smp][ok] / vol[smp][ok, None]
-        b_orc = r["mom"][ok] / r["vol"][ok, None]
-        brel = np.linalg.norm(b_gpu - b_orc, axis=1) / diag
-        w = int(np.argmax(vrel))
-        sw = smp[ok][w]
+        brel = np.linalg.norm(mom[smp][ok] / vol[smp][ok, None] - r["mom"][ok] / r["vol"][ok, None], axis=1) / diag
         out.append({"iteration": it + 1, "sampled": int(ok.sum()), "vol_rel_max": float(vrel.max()),
                     "vol_rel_p99": float(np.percentile(vrel, 99)), "bary_diag_max": float(brel.max()),
-                    "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol),
-                    "tiny_cells": int(tiny.sum()), "tiny_vol_abs_max": tiny_abs,
-                    "worst_cell": {"site": pos[sw].tolist(), "vol": float(vol[sw]), "oracle_vol": float(r["vol"][ok][w]),
-                                   "kth_neighbour_dist": float(dK[ok][w])}})
-    worst = {k: max(o[k] for o in out) for k in ("vol_rel_max", "bary_diag_max", "total_vol_rel", "tiny_vol_abs_max")}
-    return {"oracle": "FP64 cell-tet restatement (oracle/), per sampled site, every tet in reach",
-            "sample_per_iteration": m, "iterations": out, "worst": worst,
-            "bars": {"vol_rel": 1e-5, "bary_diag": 1e-6, "total_vol_rel": 1e-6, "tiny_vol_abs": 1e-6},
-            "tiny": "cells below 1e-9 of the largest sampled volume: absolute error / largest volume"}
+                    "total_vol_rel": float(abs(vol.sum() - mesh_vol) / mesh_vol)})
+    worst = {k: max(o[k] for o in out) for k in ("vol_rel_max", "bary_diag_max", "total_vol_rel")}
+    return {"sample_per_iteration": m, "iterations": out, "worst": worst}
+
+
+def batch_measure(pkg, warmup, steps, device):
+    """The batched configuration: 256 Kuhn cubes iterated together."""
+    import voronoi_gb300.meshgen as mg
+    w = WORKLOADS["batch256_kuhn"]
+    t0 = time.perf_counter()
+    probs = mg.batch_problems(w["n_prob"], seed=4)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with pkg.Batch([(P.verts, P.tets, P.sites) for P in probs], site_k=0, tune_grid=True, use_graph=True,
+                   device=device) as B:
+        create_s = time.perf_counter() - t0
+        B.time_iterate(warmup, update=True)
+        ms = B.time_iterate(steps, update=True)
+        ks = collections.Counter(B.problem(p)["site_k"] for p in range(B.n_prob))
+        out = {"workload": "batch256_kuhn", "description": w["desc"], "value": round(steps / (ms / 1e3), 3),
+               "unit": UNIT, "ms_per_step": round(ms / steps, 4), "steps": steps, "warmup": warmup,
+               "n_prob": B.n_prob, "n_site": B.n_site, "n_tet": B.n_tet,
+               "sites_per_s": round(B.n_site * steps / (ms / 1e3), 1),
+               "site_k_histogram": {str(k): v for k, v in sorted(ks.items())}, "grid_density": round(B.density, 2),
+               "generate_s": round(gen_s, 1), "create_s": round(create_s, 1)}
+    return out
 
 
 def run_batch(args):
@@ -620,6 +716,48 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def reference_full_run(checker, L, P, K, iters, threads):
+    """The reference's kernels (host build) on every pair of P, timed in
+    full: per iteration its grid kNN (kn_prepare + kn_solve), the tet
+    centroids and their brute-force tet_k selection (knn_cuda_global_dev),
+    the tet-cell kernel on every (tet, slot) pair, the cell-tet kernels
+    (every site's cell, every pair) and the Lloyd update from the cell-tet
+    moments (voronoi.cu:1040-1124)."""
+    import ctypes as C
+    ptr = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+    L.ref_time_knn_grid.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    L.ref_time_knn_grid.restype = C.c_double
+    sites = np.ascontiguousarray(P.sites, np.float32).copy()
+    verts = np.ascontiguousarray(P.verts, np.float32)
+    tets = np.ascontiguousarray(P.tets, np.int32)
+    n, nt = len(sites), len(tets)
+    tk = checker.tet_k(n, nt)
+    perm = np.empty(n, np.uint32)
+    srt = np.empty((n, 3), np.float32)
+    knn = np.empty((n, K), np.uint32)
+    steps = []
+    for _ in range(iters):
+        t0 = time.perf_counter()
+        if L.ref_time_knn_grid(ptr(sites), n, ptr(perm), ptr(srt), ptr(knn), threads) < 0:
+            return None
+        cent = checker.ref_tet_centroids(verts, tets, k=K)
+        cand = np.concatenate([checker.ref_knn_brute(srt, cent, tk, q_range=(b, min(b + 8000, nt)),
+                                                     nthreads=threads, site_k=K) for b in range(0, nt, 8000)])
+        knn_i = knn.astype(np.int32)
+        checker.ref_tet_cell(srt, knn_i, verts, tets, cand, nthreads=threads)
+        vol, bary, _ = checker.ref_cell_tet(srt, knn_i, verts, tets, cand, nthreads=threads)
+        new = srt.copy()
+        nz = vol != 0
+        new[nz] = bary[nz] / vol[nz, None]
+        sites = np.ascontiguousarray(new)
+        steps.append(time.perf_counter() - t0)
+    return {"workload": "kuhn20_20k", "description": WORKLOADS["kuhn20_20k"]["desc"],
+            "value": round(1.0 / statistics.mean(steps), 4), "unit": UNIT,
+            "ms_per_step": round(statistics.mean(steps) * 1e3, 1), "steps": iters, "extrapolated": False,
+            "pairs_per_step": int(nt * tk), "cores": threads,
+            "timed": "every kernel of the reference's iteration on every site and pair (host build)"}
+
+
 def run_reference(args):
     world, rank, local = dist_env()
     if WORKLOADS[args.workload]["kind"] == "batch":
@@ -633,7 +771,7 @@ def run_reference(args):
     w = WORKLOADS[args.workload]
     load_package()
     P = make_problem(args.workload)
-    K = w["K"]
+    K = w["K"] or 64
     n, nt = len(P.sites), len(P.tets)
     tk = checker.tet_k(n, nt)
     try:
@@ -650,11 +788,13 @@ def run_reference(args):
     srt = np.empty((n, 3), np.float32)
     knn = np.empty((n, K), np.uint32)
     ptr = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
-    steps = []
+    proj, wall = [], []
     detail = None
     cand = None
+    cand_frac = 1.0
     for it in range(args.warmup + args.steps):
         timed = it >= args.warmup
+        w0 = time.perf_counter()
         t_knn = L.ref_time_knn_grid(ptr(P.sites), n, ptr(perm), ptr(srt), ptr(knn), threads)
         if t_knn < 0:
             print(json.dumps({"impl": "reference", "unavailable": "reference grid kNN needs >= ~12.7k sites"}))
@@ -662,30 +802,46 @@ def run_reference(args):
         # tet candidates: the reference's brute-force centroid kNN needs an n_tet x n_site distance matrix;
         # the same sets come from an exact grid search, timed on a sample of tets and scaled
         rows = np.arange(0, nt, max(1, nt // 20000))
+        cand_frac = len(rows) / nt
         t0 = time.perf_counter()
         checker.knn_grid(srt, cent[rows], tk, exclude_self=False, nthreads=threads)
-        t_cand = (time.perf_counter() - t0) * nt / len(rows)
+        t_cand = (time.perf_counter() - t0) / cand_frac
         if cand is None:
             cand = checker.knn_grid(srt, cent, tk, exclude_self=False, nthreads=threads)
         t_clip, detail = host_sample_baseline(checker, srt, knn.astype(np.int32), P.verts, P.tets, cand,
                                               target_s=3.0 if timed else 1.0, threads=threads)
         if timed:
-            steps.append(t_knn + t_cand + t_clip)
-    t_step = statistics.mean(steps)
+            proj.append(t_knn + t_cand + t_clip)
+            wall.append(time.perf_counter() - w0)
+    t_step = statistics.mean(proj)
     value = 1.0 / t_step
+    full = None
+    if args.workload == DEFAULT_WORKLOAD and not args.no_forms:
+        Ps = make_problem("kuhn20_20k")
+        Ls = checker.ref_lib(64)
+        full = reference_full_run(checker, Ls, Ps, 64, 2, threads)
+    sampled = detail["sample_pairs"] / (nt * tk)
     line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": round(statistics.mean(wall) * 1e3, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "description": w["desc"], "n_site": n, "n_tet": nt, "site_k": K,
                        "tet_k": tk, "parallelism": "host cores"},
             "impl": "reference",
+            "extrapolated": True,
+            "projected_ms_per_iteration": round(t_step * 1e3, 1),
+            "sampled_fraction": {"clip_pairs": round(sampled, 5), "candidate_search_tets": round(cand_frac, 6),
+                                 "grid_knn_sites": 1.0},
             "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": detail["kind"],
+                             "extrapolated": True,
                              "sample": "per step: the reference's grid kNN on all sites (host build), tet "
                                        "candidate sets (exact grid search, timed on a 1/20000 sample of tets and "
                                        "scaled), and the reference's tet-cell + cell-tet kernels on a bounded "
-                                       "sample of pairs extrapolated to all pairs",
+                                       "sample of pairs extrapolated to all pairs; ms_per_step is the measured "
+                                       "wall time of that sampled work, value the projected iteration rate",
                              "detail": detail},
             "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if full is not None:
+        line["full_run"] = full
     print(json.dumps(line), flush=True)
 
 
@@ -705,8 +861,11 @@ def main():
                          "as the reference's arithmetic filter is)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", type=int, default=0, metavar="M",
-                    help="after timing, report per-iteration error against the FP64 oracle on M sampled sites")
+                    help="also report per-iteration error against the FP64 oracle on M sampled sites")
     ap.add_argument("--accuracy-iters", type=int, default=20)
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the plain / reference / precision / batched forms and the small configuration")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched form among the extra forms")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

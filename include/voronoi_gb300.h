@@ -64,7 +64,12 @@ enum vgb_stat {
   VGB_STAT_NEEDS_EXACT = 16,    /* robust_predicates: vertex-vs-plane tests decided by
                                    the exact determinants (the reference's status
                                    needs_exact_predicates, voronoi_defs.h:10)          */
-  VGB_STAT_COUNT = 17
+  VGB_STAT_COMPLETED = 17,      /* exact form: sites whose K neighbours left their cell
+                                   unresolved, completed by every site within twice the
+                                   radius of their pieces                              */
+  VGB_STAT_UNRESOLVED = 18,     /* sites whose cell a site beyond their K nearest may
+                                   still cut (completion not possible)                 */
+  VGB_STAT_COUNT = 19
 };
 
 /* Clip kernels. */
@@ -83,8 +88,24 @@ enum vgb_buffer {
   VGB_BUF_CELL_START = 3, /* int32[grid_dim^3 + 1]                                  */
   VGB_BUF_SITE_START = 4, /* int32[n + 1]: start of each site's candidate tets      */
   VGB_BUF_SITE_TETS = 5,  /* int32[n_tet * tet_k]                                   */
-  VGB_BUF_MOMENTS = 6     /* double4[n]: volume, first moment (absolute)            */
+  VGB_BUF_MOMENTS = 6,    /* double4[n]: volume, first moment (absolute)            */
+  VGB_BUF_SITE_FLAGS = 7  /* uint8[n], cell-tet method: VGB_SITE_* bits of the last
+                             pass, grid order                                       */
 };
+
+/* Per-site outcome bits of a cell-tet pass (VGB_BUF_SITE_FLAGS). */
+#define VGB_SITE_HANDED 1   /* the one-warp pass built the cell (exact form: the first
+                               pass did not finish it; reference form: every site)   */
+#define VGB_SITE_SECMISS 2  /* the site's K neighbours did not reach its security
+                               radius (the reference's security_radius_not_reached,
+                               voronoi.cu:694-697)                                    */
+#define VGB_SITE_INTERIOR 4 /* the cell provably lies inside the mesh: taken whole    */
+#define VGB_SITE_REDO 8     /* the cell outgrew 64 vertices and was redone at 128     */
+#define VGB_SITE_DROPPED 16 /* the cell itself failed (capacity or cavity): no moments */
+#define VGB_SITE_COMPLETED 32  /* exact form: the cell's pieces reached past half the K-th
+                                  neighbour's distance, so it was clipped by every site
+                                  within twice their radius (exact where it meets the mesh) */
+#define VGB_SITE_UNRESOLVED 64 /* a site beyond the K nearest may still cut the cell      */
 
 typedef struct vgb_config {
   int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9);

@@ -1,10 +1,14 @@
 """Host build of the reference's own kernels, for pinning the oracle.
 
 TEST INFRASTRUCTURE ONLY.  This recipe reads the reference sources where they
-lie (VORONOI_REF_SRC, default /root/reference), writes generated copies of the
-few files the path needs into oracle/_ref/src/ (git-ignored, never committed:
-the reference is GPL-3.0), and compiles them for the host together with
-oracle/ref_host_driver.cpp into oracle/_ref/libref_host_k<K>.so.
+lie (the checkout named by the environment variable VORONOI_REF_SRC, or by
+--reference PATH on the command line; nothing is read without one), writes
+generated copies of the few files the path needs into oracle/_ref/src/
+(git-ignored, never committed: the reference is GPL-3.0), and compiles them
+for the host together with oracle/ref_host_driver.cpp into
+oracle/_ref/libref_host_k<K>.so.  It also copies the reference's one input
+fixture, data/joint.tet and data/joint.xyz, into oracle/_ref/data/ (also
+git-ignored), where the tests that run the CLI and the engine on it find it.
 
 Generated files:
   * voronoi.h, voronoi_defs.h, knearests.h, stopwatch.h, extern/kNN-CUDA/knncuda.h
@@ -41,15 +45,26 @@ SLICES = [
 ]
 
 
-def ref_root() -> Path:
-    return Path(os.environ.get("VORONOI_REF_SRC", "/root/reference"))
+DATA = OUT / "data"
+DATA_FILES = ["data/joint.tet", "data/joint.xyz"]
+
+
+def ref_root() -> Path | None:
+    """The reference checkout named by VORONOI_REF_SRC, or None."""
+    r = os.environ.get("VORONOI_REF_SRC", "")
+    return Path(r) if r else None
 
 
 def generate() -> bool:
-    """Write oracle/_ref/src from the reference sources; False if they are absent."""
+    """Write oracle/_ref/src (and oracle/_ref/data) from the reference; False
+    when no reference checkout is named or it is absent."""
     ref = ref_root()
-    if not (ref / "voronoi.cu").is_file():
+    if ref is None or not (ref / "voronoi.cu").is_file():
         return False
+    DATA.mkdir(parents=True, exist_ok=True)
+    for rel in DATA_FILES:
+        if (ref / rel).is_file():
+            (DATA / Path(rel).name).write_bytes((ref / rel).read_bytes())
     SRC.mkdir(parents=True, exist_ok=True)
     for rel in COPIES:
         dst = SRC / rel
@@ -98,5 +113,10 @@ def build(ks=(64, 90), quiet=True) -> list[Path]:
 
 
 if __name__ == "__main__":
-    ks = [int(a) for a in sys.argv[1:]] or [64, 90]
+    args = sys.argv[1:]
+    if "--reference" in args:
+        i = args.index("--reference")
+        os.environ["VORONOI_REF_SRC"] = args[i + 1]
+        del args[i:i + 2]
+    ks = [int(a) for a in args] or [64, 90]
     print("\n".join(str(p) for p in build(ks)))

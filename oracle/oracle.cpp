@@ -801,9 +801,23 @@ void orc_tet_cell(int mode, const float* sites, int n, const int* nbr, int K, co
 // clips that cell by the tet's four faces (voronoi.cu:620-645, 703-726).  A
 // cell whose construction failed contributes nothing (the reference then reads
 // a stale cell record).
+// reach2 (optional, n doubles): per site, the largest squared distance from
+// the site to a vertex of its contributing pieces (cell ^ tet).  Every site
+// that can clip the site's clipped cell lies within twice that distance, so
+// a neighbour list holding all sites that near is complete for the cell.
+void orc_cell_tet_ex(int mode, const float* sites, int n, const int* nbr, int K, const float* verts,
+                     const int* tets, int nt, const int* cand, int tk, double* vol, double* mom,
+                     long long* hist, double* reach2, int nthreads);
+
 void orc_cell_tet(int mode, const float* sites, int n, const int* nbr, int K, const float* verts,
                   const int* tets, int nt, const int* cand, int tk, double* vol, double* mom,
                   long long* hist, int nthreads) {
+  orc_cell_tet_ex(mode, sites, n, nbr, K, verts, tets, nt, cand, tk, vol, mom, hist, nullptr, nthreads);
+}
+
+void orc_cell_tet_ex(int mode, const float* sites, int n, const int* nbr, int K, const float* verts,
+                     const int* tets, int nt, const int* cand, int tk, double* vol, double* mom,
+                     long long* hist, double* reach2, int nthreads) {
   std::memset(vol, 0, sizeof(double) * n);
   std::memset(mom, 0, sizeof(double) * 3 * n);
   for (int i = 0; i < 14; ++i) hist[i] = 0;
@@ -835,6 +849,7 @@ void orc_cell_tet(int mode, const float* sites, int n, const int* nbr, int K, co
     std::vector<R> pv(npairs, R(0));
     std::vector<V4<R>> pm(npairs);
     std::vector<int> code(npairs);
+    std::vector<double> pr2(reach2 ? npairs : 0, 0.0);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 256)
 #endif
@@ -861,6 +876,19 @@ void orc_cell_tet(int mode, const float* sites, int n, const int* nbr, int K, co
       pv[p] = v;
       pm[p] = m;
       code[p] = c.status + 100;
+      if (reach2) {
+        double r2 = 0.0;
+        for (int i = 0; i < c.nt; ++i) {
+          V4<R> d = sub4(c.vertex(i), c.seed);
+          r2 = std::max(r2, (double)dot3(d, d));
+        }
+        pr2[p] = r2;
+      }
+    }
+    if (reach2) {
+      for (int i = 0; i < n; ++i) reach2[i] = 0.0;
+      for (long long p = 0; p < npairs; ++p)
+        if (contributed(code[p])) reach2[cand[p]] = std::max(reach2[cand[p]], pr2[p]);
     }
     if (SH) {
       std::vector<float> fv(n, 0.f), fm(3 * (size_t)n, 0.f);

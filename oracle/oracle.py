@@ -68,6 +68,7 @@ def lib():
         L.orc_tet_k.restype = i
         L.orc_tet_cell.argtypes = [i, vp, i, vp, i, vp, vp, i, vp, i, vp, vp, vp, vp, vp, i]
         L.orc_cell_tet.argtypes = [i, vp, i, vp, i, vp, vp, i, vp, i, vp, vp, vp, i]
+        L.orc_cell_tet_ex.argtypes = [i, vp, i, vp, i, vp, vp, i, vp, i, vp, vp, vp, vp, i]
         L.orc_lloyd_update.argtypes = [i, vp, i, vp, vp]
         L.orc_mesh_volume.argtypes = [vp, vp, i]
         L.orc_mesh_volume.restype = d
@@ -158,16 +159,23 @@ def tet_cell(sites, nbr, verts, tets, cand, mode: int = FIXED, pair_status: bool
     return out
 
 
-def cell_tet(sites, nbr, verts, tets, cand, mode: int = FIXED, nthreads: int = 0):
+def cell_tet(sites, nbr, verts, tets, cand, mode: int = FIXED, nthreads: int = 0, reach: bool = False):
+    """Cell-tet method over all candidate pairs.  reach=True adds reach2 (n,):
+    the largest squared distance from each site to a vertex of its
+    contributing pieces."""
     sites, nbr, verts, tets, cand = _f32(sites), _i32(nbr), _f32(verts), _i32(tets), _i32(cand)
     n, K = nbr.shape
     nt, tk = cand.shape
     vol = np.zeros(n, np.float64)
     mom = np.zeros((n, 3), np.float64)
     hist = np.zeros(14, np.int64)
-    lib().orc_cell_tet(mode, _p(sites), n, _p(nbr), K, _p(verts), _p(tets), nt, _p(cand), tk,
-                       _p(vol), _p(mom), _p(hist), nthreads)
-    return dict(vol=vol, mom=mom, hist=hist)
+    r2 = np.zeros(n, np.float64) if reach else None
+    lib().orc_cell_tet_ex(mode, _p(sites), n, _p(nbr), K, _p(verts), _p(tets), nt, _p(cand), tk,
+                          _p(vol), _p(mom), _p(hist), _p(r2), nthreads)
+    out = dict(vol=vol, mom=mom, hist=hist)
+    if reach:
+        out["reach2"] = r2
+    return out
 
 
 def sample_cells(sites, sample, nbr, verts, tets, reach, mode: int = FIXED, nthreads: int = 0):
@@ -196,8 +204,92 @@ def sample_cells(sites, sample, nbr, verts, tets, reach, mode: int = FIXED, nthr
     hits = tree.query_ball_point(s2[:m], np.asarray(reach, np.float64) + float(rt.max()) * 1.001 + 1e-3)
     pt = np.concatenate([np.asarray(h, np.int64) for h in hits]) if m else np.zeros(0, np.int64)
     ps = np.repeat(np.arange(m), [len(h) for h in hits]).astype(np.int32)
-    r = cell_tet(s2, nbr2, verts, tets[pt], ps.reshape(-1, 1), mode=mode, nthreads=nthreads)
-    return dict(vol=r["vol"], mom=r["mom"], pairs=len(pt))
+    r = cell_tet(s2, nbr2, verts, tets[pt], ps.reshape(-1, 1), mode=mode, nthreads=nthreads, reach=True)
+    return dict(vol=r["vol"], mom=r["mom"], pairs=len(pt), reach2=r["reach2"])
+
+
+def tet_reach(sites, verts, tets):
+    """Per tet: (centroid, reach) with reach = d1 + 2 r, d1 the distance from
+    the tet's centroid to its nearest site and r its largest corner distance
+    from the centroid.  A site whose Voronoi cell meets the tet lies within
+    reach of the centroid: a point x of the tet has the centroid's nearest
+    site within r + d1, so the site owning x is at most that far from x and
+    at most r farther from the centroid."""
+    from scipy.spatial import cKDTree
+    corners = _f32(verts)[_i32(tets)].astype(np.float64)   # (nt, 4, 3)
+    cent = corners.mean(axis=1)
+    rt = np.sqrt(((corners - cent[:, None, :]) ** 2).sum(-1)).max(1)
+    d1, _ = cKDTree(_f32(sites).astype(np.float64)).query(cent, 1)
+    return cent, (d1 + 2.0 * rt) * (1.0 + 1e-6) + 1e-3
+
+
+def complete_cells(sites, sample, verts, tets, k0: int = 128, kmax: int = 4096, mode: int = FIXED,
+                   nthreads: int = 0, reach=None):
+    """The exact clipped cells of a sample of the sites, with neighbour lists
+    complete for each cell whatever any engine's K.
+
+    Candidate tets of a sampled site: every tet whose centroid lies within
+    the tet's reach of the site (tet_reach: complete for the true cell).
+    Neighbours: the k nearest sites by (distance, index), self excluded,
+    starting at k0.  With that list the cell's pieces lie within R of the
+    site (R from the oracle's own pieces); a site that could still cut the
+    true cell lies within 2R, so a list whose last neighbour is farther than
+    2R is complete.  Sites whose list is not are evaluated again with four
+    times the neighbours, up to kmax.  Returns dict(vol (m,), mom (m,3), k
+    (neighbours used), complete (bool per site), pairs)."""
+    from scipy.spatial import cKDTree
+    sites, verts, tets = _f32(sites), _f32(verts), _i32(tets)
+    sample = np.asarray(sample, np.int64)
+    n, m = len(sites), len(sample)
+    cent, tr = reach if reach is not None else tet_reach(sites, verts, tets)
+    ctree = cKDTree(cent)
+    stree = cKDTree(sites.astype(np.float64))
+    rmax = float(tr.max())
+    vol = np.zeros(m)
+    mom = np.zeros((m, 3))
+    used = np.zeros(m, np.int64)
+    done = np.zeros(m, bool)
+    todo = np.arange(m)
+    k = k0
+    npairs = 0
+    while len(todo):
+        kk = min(k, n - 1)
+        q = sample[todo]
+        dist, nb = stree.query(sites[q].astype(np.float64), kk + 1)
+        dist, nb = dist.reshape(len(q), kk + 1), nb.reshape(len(q), kk + 1)
+        keep = nb != q[:, None]                      # self out, by index (duplicates stay)
+        keep[keep.sum(1) > kk, -1] = False
+        nbr = nb[keep].reshape(len(q), kk)
+        dk = dist[keep].reshape(len(q), kk)[:, -1]
+        # the sampled sites first, then the rest (the oracle builds cells for
+        # the first rows only)
+        order = np.concatenate([q, np.setdiff1d(np.arange(n), q)])
+        pos = np.empty(n, np.int64)
+        pos[order] = np.arange(n)
+        s2 = sites[order]
+        nbr2 = pos[nbr].astype(np.int32)
+        hits = ctree.query_ball_point(sites[q].astype(np.float64), rmax)
+        pt, ps = [], []
+        for i, h in enumerate(hits):
+            h = np.asarray(h, np.int64)
+            if len(h):
+                h = h[np.linalg.norm(cent[h] - sites[q[i]], axis=1) <= tr[h]]
+            pt.append(h)
+            ps.append(np.full(len(h), i, np.int32))
+        pt = np.concatenate(pt) if pt else np.zeros(0, np.int64)
+        ps = np.concatenate(ps) if ps else np.zeros(0, np.int32)
+        npairs += len(pt)
+        r = cell_tet(s2, nbr2, verts, tets[pt], ps.reshape(-1, 1), mode=mode, nthreads=nthreads, reach=True)
+        R = np.sqrt(r["reach2"])
+        comp = (dk > 2.0 * R * (1.0 + 1e-6) + 1e-3) | (kk == n - 1)
+        ok = comp | (kk >= kmax)
+        vol[todo[ok]] = r["vol"][ok]
+        mom[todo[ok]] = r["mom"][ok]
+        used[todo[ok]] = kk
+        done[todo[ok]] = comp[ok]
+        todo = todo[~ok]
+        k *= 4
+    return dict(vol=vol, mom=mom, k=used, complete=done, pairs=npairs)
 
 
 def lloyd_update(sites, vol, mom, mode: int = FIXED):

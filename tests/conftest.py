@@ -8,7 +8,9 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 PKG_DIR = ROOT / "3d-voronoi-gpu_gb300"
 GOLDEN = ROOT / "tests" / "golden"
-REF_DATA = Path("/root/reference/data")
+# the reference's input fixture (data/joint.tet, data/joint.xyz), copied by
+# oracle/make_ref.py into the git-ignored oracle/_ref/data/
+REF_DATA = ROOT / "oracle" / "_ref" / "data"
 
 sys.path.insert(0, str(ROOT / "oracle"))
 

@@ -1,9 +1,9 @@
 """Generate the golden fixtures of tests/golden/ from the reference's own kernels.
 
-Run in a container where the reference sources are present (the recipe in
-oracle/make_ref.py host-compiles them):
+Run where a reference checkout is present, naming it (the recipe in
+oracle/make_ref.py host-compiles its kernels and copies its joint fixture):
 
-    python tests/golden/make_golden.py
+    VORONOI_REF_SRC=<reference checkout> python tests/golden/make_golden.py
 
 Every fixture stores its inputs (or how to regenerate them deterministically)
 and the outputs of the reference kernels run serially on the host, in the
@@ -82,9 +82,9 @@ def cfg1_cube(mg):
     np.savez_compressed(ROOT / "tests/golden/cube20_s20000_k64.npz", **out)
 
 
-def joint(mg, ref_root=Path("/root/reference")):
-    v, t = mg.read_tet(str(ref_root / "data/joint.tet"))
-    s = mg.read_xyz(str(ref_root / "data/joint.xyz"))
+def joint(mg, data=ROOT / "oracle" / "_ref" / "data"):
+    v, t = mg.read_tet(str(data / "joint.tet"))
+    s = mg.read_xyz(str(data / "joint.xyz"))
     K = 90
     full = O.ref_knn_brute(s, s, K + 1)
     assert (full[:, 0] == np.arange(len(s))).all()
@@ -101,6 +101,12 @@ def joint(mg, ref_root=Path("/root/reference")):
 
 
 if __name__ == "__main__":
+    spec = importlib.util.spec_from_file_location("_make_ref", ROOT / "oracle" / "make_ref.py")
+    mr = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mr)
+    if not mr.generate():
+        sys.exit("set VORONOI_REF_SRC to the reference checkout")
+    mr.build([64, 90])
     mg = _meshgen()
     small_cube(mg)
     cfg1_cube(mg)

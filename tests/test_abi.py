@@ -40,6 +40,17 @@ def test_library_exports_every_declared_symbol(built):
     assert not missing, missing
 
 
+def test_library_exports_the_reference_headers_cxx_names(built):
+    """The reference's knearests.h declares the kn_* functions with C++
+    linkage (knearests.h:20-27): the library exports those mangled names too,
+    so objects compiled against that header link unchanged."""
+    lib = ctypes.CDLL(str(built))
+    for sym in ["_Z10kn_prepareP6float3i", "_Z8kn_solveP10kn_problem", "_Z7kn_freePP10kn_problem",
+                "_Z14kn_print_statsP10kn_problem", "_Z13kn_get_pointsP10kn_problem",
+                "_Z16kn_get_knearestsP10kn_problem", "_Z18kn_get_permutationP10kn_problem"]:
+        assert hasattr(lib, sym), sym
+
+
 def test_build_targets_sm103a_only():
     text = (ROOT / "3d-voronoi-gpu_gb300" / "build.py").read_text()
     archs = set(re.findall(r"arch=compute_(\w+),code=sm_(\w+)", text))

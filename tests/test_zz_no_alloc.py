@@ -3,8 +3,9 @@ memory (a framework owning the device memory pool, or a loop that cannot
 afford cudaMalloc's implicit device synchronisation).  Its intermediate
 arrays live in a static device array; the caller only passes device buffers
 for the points and the results.  Checked through the C ABI against the
-allocating entry point (kn_prepare_k + kn_solve), bit for bit, on two calls
-in a row that reuse the same static array.  This file sorts last so that a
+allocating entry point (kn_prepare_k + kn_solve), bit for bit, on three calls
+in a row that reuse the same static array (the last at the size limit, on a
+non-default stream).  This file sorts last so that a
 run stopping at the first failure has run every other test first."""
 import ctypes
 
@@ -32,16 +33,23 @@ def test_noalloc_knn_matches_allocating_entry_point(pkg):
     pkg.build()
     f = _noalloc(pkg)
     dev = torch.device("cuda:0")
-    # two calls in a row on the shared static array: a larger problem after a
-    # smaller one, so stale cell counts from the first would show
-    for seed, n, k in [(11, 6000, 32), (12, 40000, 64)]:
+    # calls in a row on the shared static array: larger problems after
+    # smaller ones, so stale cell counts from an earlier call would show; the
+    # last is the largest size the array takes (grid side 28, the largest
+    # work area) with K = 128 (four key slots per lane), on a stream of the
+    # caller's own
+    side = torch.cuda.Stream(device=dev)
+    for seed, n, k, stream in [(11, 6000, 32, None), (12, 40000, 64, None), (13, 65536, 128, side)]:
         pts = _points(seed, n)
         d_pts = torch.from_numpy(pts).to(dev)
         d_knn = torch.full((n, k), -1, dtype=torch.int32, device=dev)
         d_perm = torch.full((n,), -1, dtype=torch.int32, device=dev)
         torch.cuda.synchronize()
-        rc = f(d_pts.data_ptr(), n, k, d_knn.data_ptr(), d_perm.data_ptr(), None)
+        rc = f(d_pts.data_ptr(), n, k, d_knn.data_ptr(), d_perm.data_ptr(),
+               stream.cuda_stream if stream is not None else None)
         assert rc == 0, pkg.lib().vgb_last_error().decode()
+        if stream is not None:
+            stream.synchronize()
         torch.cuda.synchronize()
         kn = pkg.KnProblem(pts, k=k)
         kn.solve()
