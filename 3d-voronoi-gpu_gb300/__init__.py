@@ -37,6 +37,7 @@ BUFFERS = {"sites": 0, "knn": 1, "cand": 2, "cell_start": 3, "site_start": 4, "s
 # per-site outcome bits of a cell-tet pass (buffer "site_flags")
 SITE_HANDED, SITE_SECMISS, SITE_INTERIOR, SITE_REDO, SITE_DROPPED, SITE_COMPLETED, SITE_UNRESOLVED = (
     1, 2, 4, 8, 16, 32, 64)
+SITE_SCAN_FAILED = 128
 METHODS = {"site_major": 0, "plain": 1, "cell_tet": 2}
 STAT_COUNT = 19
 
@@ -56,7 +57,8 @@ def build(force: bool = False) -> Path:
 
 class _Config(C.Structure):
     _fields_ = [("site_k", C.c_int), ("tet_k", C.c_int), ("grid_dim", C.c_int), ("method", C.c_int),
-                ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int), ("robust_predicates", C.c_int)]
+                ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int), ("robust_predicates", C.c_int),
+                ("autotune", C.c_int)]
 
 
 class _KnProblem(C.Structure):
@@ -103,6 +105,8 @@ def lib() -> C.CDLL:
     L.vgb_engine_phase_ms.argtypes = [vp, C.POINTER(C.c_float)]
     L.vgb_engine_time_iterate.argtypes = [vp, i, i, C.POINTER(C.c_float)]
     L.vgb_engine_set_graph.argtypes = [vp, i]
+    L.vgb_engine_shape.argtypes = [vp, ip, ip, ip]
+    L.vgb_batch_shape.argtypes = [vp, ip, ip, ip]
     L.vgb_host_alloc.argtypes = [sz]
     L.vgb_host_alloc.restype = vp
     L.vgb_host_free.argtypes = [vp]
@@ -179,7 +183,7 @@ class Engine:
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
                  method: str = "cell_tet", use_graph: bool = True, device: int = 0, exact: bool = False,
-                 robust_predicates: bool = False):
+                 robust_predicates: bool = False, autotune: bool = False):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -192,6 +196,7 @@ class Engine:
         cfg.method, cfg.use_graph, cfg.device = METHODS[method], int(use_graph), device
         cfg.exact = int(exact)
         cfg.robust_predicates = int(robust_predicates)
+        cfg.autotune = int(autotune)
         h = C.c_void_p()
         _check(L.vgb_engine_create(C.byref(h), C.byref(cfg), _p(self._verts), len(self._verts), _p(self._tets),
                                    len(self._tets), _p(s), len(s)), "vgb_engine_create")
@@ -220,6 +225,13 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+    def shape(self) -> dict:
+        """Launch shapes in use: kNN warps per block, first-pass lanes per
+        site, one-warp pass vertex capacity."""
+        v = [C.c_int() for _ in range(3)]
+        _check(lib().vgb_engine_shape(self._h, *[C.byref(x) for x in v]), "vgb_engine_shape")
+        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value}
 
     def set_sites(self, sites):
         s = _f32(sites)
@@ -353,6 +365,12 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+    def shape(self) -> dict:
+        """Launch shapes the autotuner kept (see Engine.shape)."""
+        v = [C.c_int() for _ in range(3)]
+        _check(lib().vgb_batch_shape(self._h, *[C.byref(x) for x in v]), "vgb_batch_shape")
+        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value}
 
     def problem(self, p: int) -> dict:
         """Sizes and tuned parameters of problem p."""

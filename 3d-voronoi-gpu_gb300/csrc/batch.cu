@@ -44,6 +44,7 @@ struct vgb_batch {
   long long ncell = 0, ncell_cap = 0, knn_cap = 0;
   int kmax = 0;
   float density = 3.1f;          // sites per grid cell
+  vgb::KernelShape shape{};      // launch shapes (autotuned with the grid density)
   ProbDesc* d_probs = nullptr;
   int* site_prob = nullptr;
   int* tet_prob = nullptr;
@@ -161,7 +162,7 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   // KNN_TIER neighbours first; the rest for the sites that need them (clip phase)
   const int tier = b->kmax > KNN_TIER ? KNN_TIER : 0;
   if (knn_sites(b->sites, b->n, b->cell_start, b->d_probs, b->site_prob, none, b->kmax, b->pos_of_id, b->knn,
-                b->redo_count + 5, st, tier))
+                b->redo_count + 5, st, tier, b->shape.knn_warps))
     return VGB_ERR_CUDA;
   if (tet_reach(b->sites, b->cell_start, b->d_probs, b->tet_prob, none, b->n_prob, b->tet_sph, b->n_tet, b->reach,
                 b->reach_max, st))
@@ -171,7 +172,8 @@ int batch_pass(vgb_batch* b, int update, bool count_secmiss) {
   if (clip_site_major(true, b->sites, b->n, b->knn, b->d_probs, b->site_prob, none, b->verts, b->tets, nullptr,
                       nullptr, b->mom, b->stats, b->field, b->field_sat, b->tet_order, b->tet_cell_start, b->tet_sph,
                       b->reach, b->reach_max, count_secmiss ? b->secmiss : nullptr, b->redo_list, b->redo_count,
-                      b->kmax, b->store, tier, b->cell_start, b->pos_of_id, b->cfg.robust_predicates != 0, st))
+                      b->kmax, b->store, tier, b->cell_start, b->pos_of_id, b->cfg.robust_predicates != 0, b->shape,
+                      st))
     return VGB_ERR_CUDA;
   if (finish_sites(b->sites, b->n, b->mom, update, st)) return VGB_ERR_CUDA;
   return VGB_OK;
@@ -427,26 +429,53 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     }
   }
   if (cfg.grid_dim == 0) {
-    // grid density: the fastest of three, timed over two passes each
+    // two passes timed after one untimed, on the current layout
+    auto timed = [&](float* ms) {
+      int r0 = batch_pass(b, 0, false);
+      if (r0) return r0;
+      cudaError_t te = cudaEventRecord(b->tev[0], b->st);
+      for (int r = 0; r < 2 && te == cudaSuccess && r0 == VGB_OK; ++r) r0 = batch_pass(b, 0, false);
+      if (te == cudaSuccess) te = cudaEventRecord(b->tev[1], b->st);
+      if (te == cudaSuccess) te = cudaEventSynchronize(b->tev[1]);
+      if (te == cudaSuccess) te = cudaEventElapsedTime(ms, b->tev[0], b->tev[1]);
+      if (!r0 && te != cudaSuccess) {
+        set_error("autotune timing: %s", cudaGetErrorString(te));
+        r0 = VGB_ERR_CUDA;
+      }
+      return r0;
+    };
+    // grid density: the fastest of three
     static const float dens[] = {1.5f, 3.1f, 6.0f};
     float best_ms = 1e30f, best = 3.1f;
     for (float d : dens) {
       b->density = d;
-      if ((rc = layout(b)) || (rc = batch_pass(b, 0, false))) { free_batch(b); return rc; }
       float ms = 0.f;
-      ce = cudaEventRecord(b->tev[0], b->st);
-      for (int r = 0; r < 2 && ce == cudaSuccess && rc == VGB_OK; ++r) rc = batch_pass(b, 0, false);
-      if (ce == cudaSuccess) ce = cudaEventRecord(b->tev[1], b->st);
-      if (ce == cudaSuccess) ce = cudaEventSynchronize(b->tev[1]);
-      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, b->tev[0], b->tev[1]);
-      if (rc || ce != cudaSuccess) {
-        if (!rc) set_error("autotune timing: %s", cudaGetErrorString(ce));
-        free_batch(b);
-        return rc ? rc : VGB_ERR_CUDA;
-      }
+      if ((rc = layout(b)) || (rc = timed(&ms))) { free_batch(b); return rc; }
       if (ms < best_ms) { best_ms = ms; best = d; }
     }
     b->density = best;
+    if ((rc = layout(b))) { free_batch(b); return rc; }
+    // launch shapes: the four clip shapes (first-pass lane groups of 8 or
+    // 16, one-warp pass of 64 or 96 vertices) with 8-warp kNN blocks, then
+    // the fastest with 4-warp kNN blocks
+    static const int shapes[4][2] = {{8, 2}, {16, 2}, {8, 3}, {16, 3}};
+    vgb::KernelShape bs{};
+    float bms = 1e30f;
+    for (auto& sh : shapes) {
+      vgb::KernelShape t{};
+      t.build_g = sh[0];
+      t.fast_sl = sh[1];
+      b->shape = t;
+      float ms = 0.f;
+      if ((rc = timed(&ms))) { free_batch(b); return rc; }
+      if (ms < bms) { bms = ms; bs = t; }
+    }
+    vgb::KernelShape t = bs;
+    t.knn_warps = 4;
+    b->shape = t;
+    float ms = 0.f;
+    if ((rc = timed(&ms))) { free_batch(b); return rc; }
+    b->shape = ms < bms ? t : bs;
   }
   if ((rc = layout(b))) { free_batch(b); return rc; }
   *out = b;
@@ -489,6 +518,14 @@ int vgb_batch_time_iterate(vgb_batch* b, int n_iter, int update, float* ms) {
   VGB_CUDA_TRY(cudaEventRecord(b->tev[1], b->st));
   VGB_CUDA_TRY(cudaEventSynchronize(b->tev[1]));
   VGB_CUDA_TRY(cudaEventElapsedTime(ms, b->tev[0], b->tev[1]));
+  return VGB_OK;
+}
+
+int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots) {
+  if (!b) { set_error("NULL batch"); return VGB_ERR_INVALID; }
+  if (knn_warps) *knn_warps = b->shape.knn_warps;
+  if (build_lanes) *build_lanes = b->shape.build_g;
+  if (fast_slots) *fast_slots = b->shape.fast_sl;
   return VGB_OK;
 }
 

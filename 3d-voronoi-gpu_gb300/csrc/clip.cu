@@ -18,16 +18,16 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, co
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                     const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
-                    bool robust, cudaStream_t st) {
+                    bool robust, const KernelShape& shape, cudaStream_t st) {
   if (robust)
     return ClipPasses<true>::run(cell_tet, sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets,
                                  mom, stats, field, field_sat, tet_order, tet_cell_start, tet_sph, reach,
                                  reach_max_bits, prob_secmiss, lists, counters, kmax, store, k_tier, cell_start,
-                                 pos_of_id, st);
+                                 pos_of_id, shape, st);
   return ClipPasses<false>::run(cell_tet, sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets,
                                 mom, stats, field, field_sat, tet_order, tet_cell_start, tet_sph, reach,
                                 reach_max_bits, prob_secmiss, lists, counters, kmax, store, k_tier, cell_start,
-                                pos_of_id, st);
+                                pos_of_id, shape, st);
 }
 
 // Clear radius of the inside field: an inside cell's byte becomes 1 + the

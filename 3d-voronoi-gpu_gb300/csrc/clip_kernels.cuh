@@ -89,14 +89,19 @@ enum WarpCount : int {
   WC_UNRESOLVED, WC_N
 };
 // Each per-warp count goes to the counter slot of the same index.
-static_assert(WC_CAND == STAT_CANDIDATES && WC_CULLED == STAT_CULLED && WC_CLIPPED == STAT_CLIPPED &&
-                  WC_EMPTY == STAT_EMPTY && WC_CONTRIB == STAT_CONTRIB && WC_SECMISS == STAT_SECURITY_MISS &&
-                  WC_OVERFLOW == STAT_TRI_OVERFLOW && WC_BOUNDARY == STAT_BOUNDARY_FAIL && WC_PLANES == STAT_PLANES &&
-                  WC_CLIPS == STAT_CLIPS && WC_FINAL == STAT_FINAL_VERTICES && WC_CONFLICT == STAT_CONFLICT_TESTS &&
-                  WC_CULLTESTS == STAT_CULL_TESTS && WC_NEWV == STAT_NEW_VERTICES && WC_INTERIOR == STAT_INTERIOR &&
-                  WC_REDO == STAT_REDO && WC_EXACT == STAT_NEEDS_EXACT && WC_COMPLETED == STAT_COMPLETED &&
-                  WC_UNRESOLVED == STAT_UNRESOLVED && WC_N == STAT_COUNT,
-              "per-warp counts and counter slots in the same order");
+constexpr bool same_slots() {
+  constexpr int wc[] = {WC_CAND, WC_CULLED, WC_CLIPPED, WC_EMPTY, WC_CONTRIB, WC_SECMISS, WC_OVERFLOW, WC_BOUNDARY,
+                        WC_PLANES, WC_CLIPS, WC_FINAL, WC_CONFLICT, WC_CULLTESTS, WC_NEWV, WC_INTERIOR, WC_REDO,
+                        WC_EXACT, WC_COMPLETED, WC_UNRESOLVED, WC_N};
+  constexpr int st[] = {STAT_CANDIDATES, STAT_CULLED, STAT_CLIPPED, STAT_EMPTY, STAT_CONTRIB, STAT_SECURITY_MISS,
+                        STAT_TRI_OVERFLOW, STAT_BOUNDARY_FAIL, STAT_PLANES, STAT_CLIPS, STAT_FINAL_VERTICES,
+                        STAT_CONFLICT_TESTS, STAT_CULL_TESTS, STAT_NEW_VERTICES, STAT_INTERIOR, STAT_REDO,
+                        STAT_NEEDS_EXACT, STAT_COMPLETED, STAT_UNRESOLVED, STAT_COUNT};
+  for (int i = 0; i < (int)(sizeof(wc) / sizeof(wc[0])); ++i)
+    if (wc[i] != st[i]) return false;
+  return true;
+}
+static_assert(same_slots(), "per-warp counts and counter slots in the same order");
 __device__ __forceinline__ int stat_slot(int w) { return w; }
 
 // Plane slots of a site's shared state: 0..3 tet faces, 4+j bisector j,
@@ -736,11 +741,14 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
                       nfar = gather_far();
                     } else if (r != CLIP_NONE) {
                       fail = true;
+                      if (lane == 0 && (r == CLIP_OVERFLOW || r == CLIP_BOUNDARY))
+                        S.cnt[r == CLIP_OVERFLOW ? WC_OVERFLOW : WC_BOUNDARY]++;
                     }
                   }
                 }
               }
           cdone = !fail;
+          if (!cdone && lane == 0) S.site_flags |= SITE_SCAN_FAILED;
         }
         const bool miss_left = secmiss && !cdone;
         // (counted once the site is done: a site handed to the 128-vertex
@@ -1143,6 +1151,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_BUILD_MIN_BLOCKS) k_bui
 constexpr int BUILD_G = 8, BUILD_SL = 4;
 static_assert(BUILD_G * BUILD_SL <= STORE_VERTS, "a stored cell holds a first-pass cell");
 constexpr int SLOTS_FAST = 2, SLOTS_REDO = 4, SLOTS_TET_CELL = 3;
+// The autotuner's alternative one-warp pass: 96 vertices per cell.
+constexpr int SLOTS_WIDE = 3;
 // The completion pass (rare sites, often beside dense clusters: many faces)
 // runs with 256 vertices per cell.
 constexpr int SLOTS_COMPLETE = 8;
@@ -1155,9 +1165,9 @@ inline int resident_blocks(F kernel, int sms, int* out, size_t dyn_smem = 0) {
   return 0;
 }
 
-// k_build's dynamic shared memory (its groups' planes)
-inline size_t build_dyn_smem(int kmax) {
-  return sizeof(float4) * (size_t)(CLIP_WARPS * (WARP / BUILD_G)) * build_plane_stride(kmax);
+// k_build's dynamic shared memory (its groups' planes) with groups of G lanes
+inline size_t build_dyn_smem(int kmax, int G = BUILD_G) {
+  return sizeof(float4) * (size_t)(CLIP_WARPS * (WARP / G)) * build_plane_stride(kmax);
 }
 
 // The clip passes with float (R = false) or robust (R = true) predicates.
@@ -1166,13 +1176,14 @@ inline size_t build_dyn_smem(int kmax) {
 template <bool R>
 struct ClipPasses {
   // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
-  // fast / redo, cell-tet batched fast / redo, completion lone / batched
+  // fast / redo, cell-tet batched fast / redo, completion lone / batched,
+  // the 96-vertex fast pass lone / batched
   static int* resident() {
-    static int r[7] = {0, 0, 0, 0, 0, 0, 0};
+    static int r[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     return r;
   }
   static int prepare();
-  static int build_blocks(bool batched, int kmax);
+  static int build_blocks(bool batched, int kmax, int G);
   static int run(bool cell_tet, const float4* sites, int n, unsigned* knn, const ProbDesc* probs,
                  const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
                  const int* site_start, const int* site_tets, dmom4* mom, unsigned long long* stats,
@@ -1180,7 +1191,7 @@ struct ClipPasses {
                  const int* tet_cell_start, const float4* tet_sph, const float* reach,
                  const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                  const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
-                 cudaStream_t st);
+                 const KernelShape& shape, cudaStream_t st);
 };
 
 template <bool R>
@@ -1195,25 +1206,32 @@ int ClipPasses<R>::prepare() {
       resident_blocks(k_clip_site<true, true, SLOTS_FAST, R>, sms, r + 3) ||
       resident_blocks(k_clip_site<true, true, SLOTS_REDO, R>, sms, r + 4) ||
       resident_blocks(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, sms, r + 5) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, sms, r + 6))
+      resident_blocks(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, sms, r + 6) ||
+      resident_blocks(k_clip_site<true, false, SLOTS_WIDE, R>, sms, r + 7) ||
+      resident_blocks(k_clip_site<true, true, SLOTS_WIDE, R>, sms, r + 8))
     return -2;
   return 0;
 }
 
-// k_build's resident blocks per largest K (lone / batched)
+// k_build's resident blocks per largest K (lone / batched, groups of 8 / 16)
 template <bool R>
-int ClipPasses<R>::build_blocks(bool batched, int kmax) {
-  static int blocks[2][MAX_SITE_K + 1] = {};
-  int& b = blocks[batched][kmax];
+int ClipPasses<R>::build_blocks(bool batched, int kmax, int G) {
+  static int blocks[2][2][MAX_SITE_K + 1] = {};
+  int& b = blocks[batched][G == 16][kmax];
   if (b == 0) {
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return 0;
-    const size_t dyn = build_dyn_smem(kmax);
-    if (batched ? resident_blocks(k_build<true, BUILD_G, BUILD_SL, R>, sms, &b, dyn)
-                : resident_blocks(k_build<false, BUILD_G, BUILD_SL, R>, sms, &b, dyn))
-      return 0;
+    const size_t dyn = build_dyn_smem(kmax, G);
+    int rc;
+    if (G == 16)
+      rc = batched ? resident_blocks(k_build<true, 16, 2, R>, sms, &b, dyn)
+                   : resident_blocks(k_build<false, 16, 2, R>, sms, &b, dyn);
+    else
+      rc = batched ? resident_blocks(k_build<true, BUILD_G, BUILD_SL, R>, sms, &b, dyn)
+                   : resident_blocks(k_build<false, BUILD_G, BUILD_SL, R>, sms, &b, dyn);
+    if (rc) return 0;
   }
   return b;
 }
@@ -1226,8 +1244,12 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
                        const int* tet_cell_start, const float4* tet_sph, const float* reach,
                        const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                        const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
-                       cudaStream_t st) {
+                       const KernelShape& shape, cudaStream_t st) {
   if (n <= 0) return 0;
+  if ((shape.build_g != 8 && shape.build_g != 16) || (shape.fast_sl != 2 && shape.fast_sl != 3)) {
+    set_error("clip: shape (%d lanes, %d slots) not built", shape.build_g, shape.fast_sl);
+    return -1;
+  }
   int* const g_clip_resident_blocks = resident();
   if (g_clip_resident_blocks[0] == 0 && prepare()) return -2;
   if (!cell_tet && probs) {
@@ -1279,35 +1301,47 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
       set_error("clip: largest K %d outside [1, %d]", kmax, MAX_SITE_K);
       return -1;
     }
-    const int bb = build_blocks(probs != nullptr, kmax);
+    const int G = shape.build_g;
+    const int bb = build_blocks(probs != nullptr, kmax, G);
     if (bb <= 0) return -2;
-    const size_t dyn = build_dyn_smem(kmax);
-    if (probs)
-      k_build<true, BUILD_G, BUILD_SL, R><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
-          cs, kt, deep, counters + 8);
-    else
-      k_build<false, BUILD_G, BUILD_SL, R><<<bb, CLIP_WARPS * WARP, dyn, st>>>(
-          sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat, counters + 2, rest, counters + 0, kmax,
-          cs, kt, deep, counters + 8);
+    const size_t dyn = build_dyn_smem(kmax, G);
+    auto build = [&](auto kernel) {
+      kernel<<<bb, CLIP_WARPS * WARP, dyn, st>>>(sites, n, knn, probs, site_prob, lone, mom, stats, field, field_sat,
+                                                  counters + 2, rest, counters + 0, kmax, cs, kt, deep,
+                                                  counters + 8);
+    };
+    if (probs) {
+      if (G == 16) build(k_build<true, 16, 2, R>);
+      else build(k_build<true, BUILD_G, BUILD_SL, R>);
+    } else {
+      if (G == 16) build(k_build<false, 16, 2, R>);
+      else build(k_build<false, BUILD_G, BUILD_SL, R>);
+    }
     // the full rows of the deep sites, before the one-warp pass reads them
     if (kt > 0 && kt < kmax &&
         knn_sites_listed(sites, n, cell_start, probs, site_prob, lone, kmax, pos_of_id, knn, deep, counters + 8,
-                         counters + 9, st))
+                         counters + 9, st, shape.knn_warps))
       return -2;
   }
   const int* in_list = exact ? rest : nullptr;
   const int* in_count = exact ? counters + 0 : nullptr;
   // exact form: the sites whose cells their K neighbours left unresolved
   // are completed last (128 vertices)
+  const bool wide = shape.fast_sl == SLOTS_WIDE;
   if (probs) {
-    launch(k_clip_site<true, true, SLOTS_FAST, R>, 3, in_list, in_count, redo, counters + 1, counters + 3);
+    if (wide)
+      launch(k_clip_site<true, true, SLOTS_WIDE, R>, 8, in_list, in_count, redo, counters + 1, counters + 3);
+    else
+      launch(k_clip_site<true, true, SLOTS_FAST, R>, 3, in_list, in_count, redo, counters + 1, counters + 3);
     launch(k_clip_site<true, true, SLOTS_REDO, R>, 4, redo, counters + 1, nullptr, nullptr, counters + 4);
     if (exact)
       launch(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, 6, esc, counters + 10, nullptr, nullptr,
              counters + 11);
   } else {
-    launch(k_clip_site<true, false, SLOTS_FAST, R>, 1, in_list, in_count, redo, counters + 1, counters + 3);
+    if (wide)
+      launch(k_clip_site<true, false, SLOTS_WIDE, R>, 7, in_list, in_count, redo, counters + 1, counters + 3);
+    else
+      launch(k_clip_site<true, false, SLOTS_FAST, R>, 1, in_list, in_count, redo, counters + 1, counters + 3);
     launch(k_clip_site<true, false, SLOTS_REDO, R>, 2, redo, counters + 1, nullptr, nullptr, counters + 4);
     if (exact)
       launch(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, 5, esc, counters + 10, nullptr, nullptr,

@@ -31,6 +31,7 @@ struct vgb_engine {
   cudaStream_t st = nullptr;
   int n_vert = 0, n_tet = 0, n = 0, K = 0, tk = 0, dim = 0;
   vgb::ProbDesc prob{};  // the engine's problem (a batch of one)
+  vgb::KernelShape shape{};  // launch shapes (autotuned when cfg.autotune)
   long long ncell = 0;
   float4* verts = nullptr;
   int4* tets = nullptr;
@@ -197,7 +198,7 @@ int run_pass(vgb_engine* e, int update) {
   // the sites that need them, in the clip phase)
   const int tier = (exact && e->cfg.method == VGB_METHOD_CELL_TET && e->K > KNN_TIER) ? KNN_TIER : 0;
   if (knn_sites(e->sites, e->n, e->cell_start, nullptr, nullptr, e->prob, e->K, e->pos_of_id, e->knn, e->redo_count + 5,
-                st, tier))
+                st, tier, e->shape.knn_warps))
     return VGB_ERR_CUDA;
   MARK(2);
   if (exact && tet_reach(e->sites, e->cell_start, nullptr, nullptr, e->prob, 1, e->tet_sph, e->n_tet, e->reach,
@@ -221,7 +222,7 @@ int run_pass(vgb_engine* e, int update) {
                         e->verts, e->tets, e->site_start, e->site_tets, e->mom, e->stats, e->field, e->field_sat,
                         exact ? e->tet_order : nullptr, exact ? e->tet_cell_start : nullptr, e->tet_sph, e->reach,
                         e->reach_max, nullptr, e->redo_list, e->redo_count, e->K, e->store, tier, e->cell_start,
-                        e->pos_of_id, e->cfg.robust_predicates != 0, st))
+                        e->pos_of_id, e->cfg.robust_predicates != 0, e->shape, st))
       return VGB_ERR_CUDA;
   } else {
     if (clip_tet_cell_plain(e->sites, e->n, e->knn, e->K, e->verts, e->tets, e->n_tet, e->cand, e->tk, e->mom_f,
@@ -237,6 +238,48 @@ int run_pass(vgb_engine* e, int update) {
   MARK(6);
 #undef MARK
   return VGB_OK;
+}
+
+// Autotuner of the launch shapes: each candidate timed over two passes (after
+// one untimed) on the current sites with CUDA events -- the four clip shapes
+// (first-pass lane groups of 8 or 16, one-warp pass of 64 or 96 vertices)
+// with 8-warp kNN blocks, then the fastest of them with 4-warp kNN blocks.
+int tune_shapes(vgb_engine* e) {
+  static const int shapes[4][2] = {{8, 2}, {16, 2}, {8, 3}, {16, 3}};
+  auto timed = [&](const KernelShape& s, float* ms) {
+    e->shape = s;
+    int rc = run_pass(e, 0);
+    if (rc) return rc;
+    VGB_CUDA_TRY(cudaEventRecord(e->tev[0], e->st));
+    for (int r = 0; r < 2 && !rc; ++r) rc = run_pass(e, 0);
+    if (rc) return rc;
+    VGB_CUDA_TRY(cudaEventRecord(e->tev[1], e->st));
+    VGB_CUDA_TRY(cudaEventSynchronize(e->tev[1]));
+    VGB_CUDA_TRY(cudaEventElapsedTime(ms, e->tev[0], e->tev[1]));
+    return VGB_OK;
+  };
+  const bool was = e->timed;
+  e->timed = false;
+  KernelShape best{};
+  float best_ms = 1e30f;
+  int rc = VGB_OK;
+  for (auto& sh : shapes) {
+    KernelShape s{};
+    s.build_g = sh[0];
+    s.fast_sl = sh[1];
+    float ms = 0.f;
+    if ((rc = timed(s, &ms))) break;
+    if (ms < best_ms) { best_ms = ms; best = s; }
+  }
+  if (!rc) {
+    KernelShape s = best;
+    s.knn_warps = 4;
+    float ms = 0.f;
+    if (!(rc = timed(s, &ms)) && ms < best_ms) best = s;
+  }
+  e->shape = best;
+  e->timed = was;
+  return rc;
 }
 
 int ensure_graph(vgb_engine* e, int update) {
@@ -280,6 +323,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->device = 0;
   cfg->exact = 0;
   cfg->robust_predicates = 0;
+  cfg->autotune = 0;
 }
 
 const char* vgb_last_error(void) { return vgb::last_error(); }
@@ -468,6 +512,9 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     }
     if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
   }
+  if (cfg.autotune && exact_form) {
+    if ((rc = tune_shapes(e)) || (rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
+  }
   *out = e;
   return VGB_OK;
 }
@@ -628,6 +675,14 @@ void* vgb_host_alloc(size_t bytes) {
 
 void vgb_host_free(void* p) {
   if (p) cudaFreeHost(p);
+}
+
+int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots) {
+  if (!e) { set_error("NULL engine"); return VGB_ERR_INVALID; }
+  if (knn_warps) *knn_warps = e->shape.knn_warps;
+  if (build_lanes) *build_lanes = e->shape.build_g;
+  if (fast_slots) *fast_slots = e->shape.fast_sl;
+  return VGB_OK;
 }
 
 int vgb_engine_info(vgb_engine* e, int* n_site, int* n_tet, int* site_k, int* tet_k, int* grid_dim) {

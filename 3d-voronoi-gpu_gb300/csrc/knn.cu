@@ -35,7 +35,6 @@
 
 namespace vgb {
 
-constexpr int KNN_WARPS = 8;  // warps (queries in flight) per CTA
 constexpr int KNN_BUF = 64;   // per-warp key buffer
 constexpr float KNN_MARGIN = 0.01f;  // in [0,1000] units; cell-assignment rounding is ~1e-4
 constexpr unsigned KFULL = 0xffffffffu;
@@ -167,10 +166,11 @@ __device__ __forceinline__ u64 kth_key(const u64 (&L)[S], int K) {
   return __shfl_sync(KFULL, v, (K - 1) & 31);
 }
 
-// Four resident CTAs per SM (32 warps): at that register budget (64 per
-// thread) the allocation spills nothing for S = 1, 2.
-template <int S, bool CENTROIDS>
-__global__ void __launch_bounds__(KNN_WARPS * 32, 4) k_knn(const float4* __restrict__ sites,
+// W warps (queries in flight) per CTA, 32 / W resident CTAs per SM (32
+// warps): at that register budget (64 per thread) the allocation spills
+// nothing for S = 1, 2.
+template <int S, bool CENTROIDS, int W>
+__global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict__ sites,
                                                         const int* __restrict__ cell_start,
                                                         const ProbDesc* __restrict__ probs,
                                                         const int* __restrict__ site_prob, ProbDesc lone,
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(KNN_WARPS * 32, 4) k_knn(const float4* __restr
                                                         unsigned* __restrict__ out, int* __restrict__ work,
                                                         int k_tier, const int* __restrict__ q_list,
                                                         const int* __restrict__ q_count) {
-  __shared__ u64 buf_all[KNN_WARPS][KNN_BUF];
+  __shared__ u64 buf_all[W][KNN_BUF];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
@@ -197,11 +197,11 @@ __global__ void __launch_bounds__(KNN_WARPS * 32, 4) k_knn(const float4* __restr
       if (lane == 0) v = atomicAdd(work, 1);
       return __shfl_sync(KFULL, v, 0);
     }
-    return cur + (int)gridDim.x * KNN_WARPS;
+    return cur + (int)gridDim.x * W;
   };
   // site queries: every site, or the sites q_list names (q_count of them)
   const int nq = (!CENTROIDS && q_list) ? *q_count : n_query;
-  for (int q = work ? next_q(0) : blockIdx.x * KNN_WARPS + wib; q < nq; q = next_q(q)) {
+  for (int q = work ? next_q(0) : blockIdx.x * W + wib; q < nq; q = next_q(q)) {
     const int qs = (!CENTROIDS && q_list) ? q_list[q] : q;
     // centroid queries belong to the lone problem
     int pq = 0;
@@ -350,85 +350,106 @@ __global__ void k_pos_of_id(const float4* __restrict__ sites, int n, const ProbD
   pos_of_id[P.site_off + site_id(sites[i])] = i;
 }
 
-// Resident CTAs of the kNN kernel (one wave) per device, set by knn_prepare
-// with that device current.  Atomic: host threads driving different devices
-// may prepare and launch at the same time.
+// Resident CTAs of the kNN kernel (one wave) per device and block shape (4
+// or 8 warps), set by knn_prepare with that device current.  Atomic: host
+// threads driving different devices may prepare and launch at the same time.
 constexpr int KNN_MAX_DEVICES = 64;
-static std::atomic<int> g_knn_blocks[KNN_MAX_DEVICES];
+static std::atomic<int> g_knn_blocks[KNN_MAX_DEVICES][2];
 
 int knn_prepare() {
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, p4 = 0, p8 = 0;
   VGB_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= KNN_MAX_DEVICES) {
     set_error("kNN: device %d beyond the supported %d", dev, KNN_MAX_DEVICES);
     return -1;
   }
   VGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn<2, false>, KNN_WARPS * 32, 0));
-  g_knn_blocks[dev].store(sms * (per_sm > 0 ? per_sm : 1));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, k_knn<2, false, 4>, 4 * 32, 0));
+  VGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p8, k_knn<2, false, 8>, 8 * 32, 0));
+  g_knn_blocks[dev][0].store(sms * (p4 > 0 ? p4 : 1));
+  g_knn_blocks[dev][1].store(sms * (p8 > 0 ? p8 : 1));
   return 0;
 }
 
-// The current device's resident kNN CTAs (prepared on first use); 0 on error.
-static int knn_blocks() {
+// The current device's resident kNN CTAs of W warps (prepared on first use);
+// 0 on error.
+static int knn_blocks(int W) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= KNN_MAX_DEVICES) {
     set_error("kNN: no usable current device");
     return 0;
   }
-  int b = g_knn_blocks[dev].load();
-  if (b == 0 && knn_prepare() == 0) b = g_knn_blocks[dev].load();
+  std::atomic<int>& slot = g_knn_blocks[dev][W == 4 ? 0 : 1];
+  int b = slot.load();
+  if (b == 0 && knn_prepare() == 0) b = slot.load();
   return b;
+}
+
+template <int S, bool CENTROIDS>
+static void launch_knn_w(int W, int blocks, cudaStream_t st, const float4* sites, const int* cell_start,
+                         const ProbDesc* probs, const int* site_prob, const ProbDesc& lone, int kq,
+                         const float4* verts, const int4* tets, const int* q_order, int n_query,
+                         const int* pos_of_id, unsigned* out, int* work, int k_tier, const int* q_list,
+                         const int* q_count) {
+  if (W == 4)
+    k_knn<S, CENTROIDS, 4><<<blocks, 4 * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts, tets,
+                                                       q_order, n_query, pos_of_id, out, work, k_tier, q_list,
+                                                       q_count);
+  else
+    k_knn<S, CENTROIDS, 8><<<blocks, 8 * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts, tets,
+                                                       q_order, n_query, pos_of_id, out, work, k_tier, q_list,
+                                                       q_count);
 }
 
 template <bool CENTROIDS>
 static int launch_knn(const float4* sites, const int* cell_start, const ProbDesc* probs, const int* site_prob,
                       const ProbDesc& lone, int kmax, int kq, const float4* verts, const int4* tets,
                       const int* q_order, int n_query, const int* pos_of_id, unsigned* out, int* work,
-                      int k_tier, const int* q_list, const int* q_count, cudaStream_t st) {
+                      int k_tier, const int* q_list, const int* q_count, cudaStream_t st, int W = 8) {
   if (kmax < 1 || kmax > 128) {
     set_error("kNN: k=%d outside [1, 128]", kmax);
     return -1;
   }
-  const int resident = knn_blocks();
+  if (W != 4 && W != 8) {
+    set_error("kNN: %d warps per block (4 or 8)", W);
+    return -1;
+  }
+  const int resident = knn_blocks(W);
   if (resident <= 0) return -1;
-  const int need = (n_query + KNN_WARPS - 1) / KNN_WARPS;
+  const int need = (n_query + W - 1) / W;
   const int want = work ? resident : 8 * resident;  // round-robin: eight waves
   const int blocks = need < want ? need : want;
   if (work) VGB_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   if (kmax <= 32)
-    k_knn<1, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work,
-                                                           k_tier, q_list, q_count);
+    launch_knn_w<1, CENTROIDS>(W, blocks, st, sites, cell_start, probs, site_prob, lone, kq, verts, tets, q_order,
+                               n_query, pos_of_id, out, work, k_tier, q_list, q_count);
   else if (kmax <= 64)
-    k_knn<2, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work,
-                                                           k_tier, q_list, q_count);
+    launch_knn_w<2, CENTROIDS>(W, blocks, st, sites, cell_start, probs, site_prob, lone, kq, verts, tets, q_order,
+                               n_query, pos_of_id, out, work, k_tier, q_list, q_count);
   else
-    k_knn<4, CENTROIDS><<<blocks, KNN_WARPS * 32, 0, st>>>(sites, cell_start, probs, site_prob, lone, kq, verts,
-                                                           tets, q_order, n_query, pos_of_id, out, work,
-                                                           k_tier, q_list, q_count);
+    launch_knn_w<4, CENTROIDS>(W, blocks, st, sites, cell_start, probs, site_prob, lone, kq, verts, tets, q_order,
+                               n_query, pos_of_id, out, work, k_tier, q_list, q_count);
   VGB_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
               const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st,
-              int k_tier) {
+              int k_tier, int knn_warps) {
   if (n <= 0) return 0;
   k_pos_of_id<<<(n + 255) / 256, 256, 0, st>>>(sites, n, probs, site_prob, lone, pos_of_id);
   VGB_CUDA_TRY(cudaGetLastError());
   const int kc = (k_tier > 0 && k_tier < kmax) ? k_tier : kmax;
   return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kc, 0, nullptr, nullptr, nullptr, n,
-                           pos_of_id, out, work, k_tier, nullptr, nullptr, st);
+                           pos_of_id, out, work, k_tier, nullptr, nullptr, st, knn_warps);
 }
 
 int knn_sites_listed(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
                      const ProbDesc& lone, int kmax, const int* pos_of_id, unsigned* out, const int* q_list,
-                     const int* q_count, int* work, cudaStream_t st) {
+                     const int* q_count, int* work, cudaStream_t st, int knn_warps) {
   if (n <= 0) return 0;
   return launch_knn<false>(sites, cell_start, probs, site_prob, lone, kmax, 0, nullptr, nullptr, nullptr, n,
-                           pos_of_id, out, work, 0, q_list, q_count, st);
+                           pos_of_id, out, work, 0, q_list, q_count, st, knn_warps);
 }
 
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,

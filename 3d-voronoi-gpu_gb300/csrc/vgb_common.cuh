@@ -142,6 +142,17 @@ const char* last_error();
 
 // --- internal launchers (all asynchronous on `st`) -------------------------
 
+// Launch shapes the autotuner may change (the defaults are the hand-picked
+// ones): warps per kNN block (queries in flight per block: 4 or 8), lanes per
+// site in the exact form's first clip pass (8 with 4 triangle slots each, or
+// 16 with 2: 32 vertices either way) and triangle slots per lane of the
+// one-warp clip pass (2 or 3: 64 or 96 vertices).
+struct KernelShape {
+  int knn_warps = 8;
+  int build_g = 8;
+  int fast_sl = 2;
+};
+
 // Exclusive scan of n ints (in may alias out).  tmp must hold scan_tmp_ints(n).
 size_t scan_tmp_ints(long long n);
 int scan_exclusive(const int* in, int* out, long long n, int* tmp, cudaStream_t st);
@@ -173,12 +184,12 @@ int grid_sort(const float4* in, float4* out, int n, long long ncell, const ProbD
 // tet_cell_start from tets_by_cell.  kmax: the largest K of the problems.
 int knn_sites(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
               const ProbDesc& lone, int kmax, int* pos_of_id, unsigned* out, int* work, cudaStream_t st,
-              int k_tier = 0);
+              int k_tier = 0, int knn_warps = 8);
 // The full K-lists of the sites q_list names (q_count of them, on the device);
 // pos_of_id as knn_sites left it.
 int knn_sites_listed(const float4* sites, int n, const int* cell_start, const ProbDesc* probs, const int* site_prob,
                      const ProbDesc& lone, int kmax, const int* pos_of_id, unsigned* out, const int* q_list,
-                     const int* q_count, int* work, cudaStream_t st);
+                     const int* q_count, int* work, cudaStream_t st, int knn_warps = 8);
 int knn_tet_centroids(const float4* sites, int n, int dim, const int* cell_start, const int* pos_of_id,
                       const float4* verts, const int4* tets, const int* tet_order, const int* tet_cell_start,
                       int n_tet, int k, unsigned* out, int* work, cudaStream_t st);
@@ -232,6 +243,7 @@ constexpr unsigned char SITE_REDO = 8;      // the cell outgrew 64 vertices and 
 constexpr unsigned char SITE_DROPPED = 16;  // the cell itself failed (capacity or cavity): no moments
 constexpr unsigned char SITE_COMPLETED = 32;   // the completion pass clipped the cell by every site that can cut it
 constexpr unsigned char SITE_UNRESOLVED = 64;  // a site beyond the K nearest may still cut the cell
+constexpr unsigned char SITE_SCAN_FAILED = 128;  // the completion's search gave up (its cell or a cut failed)
 struct CellStore {
   unsigned* tri;         // [n][STORE_VERTS]
   int* nt;               // [n]
@@ -245,7 +257,7 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, co
                     const int* tet_cell_start, const float4* tet_sph, const float* reach,
                     const unsigned* reach_max_bits, unsigned* prob_secmiss, int* lists, int* counters, int kmax,
                     const CellStore& store, int k_tier, const int* cell_start, const int* pos_of_id,
-                    bool robust, cudaStream_t st);
+                    bool robust, const KernelShape& shape, cudaStream_t st);
 // robust: the robust-predicate instantiation of the kernels.
 // prob_secmiss (optional): per-problem count of sites whose cell never
 // reached the security radius.  lists (2n ints) and counters (at least 5

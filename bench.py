@@ -336,8 +336,9 @@ def run_ours(args):
     K = w["K"]
     exact = args.method == "cell_tet" and not args.reference_form
     eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
-                     exact=exact, robust_predicates=args.robust_predicates)
+                     exact=exact, robust_predicates=args.robust_predicates, autotune=exact)
     K = eng.site_k  # the autotuned K when the workload asks for one
+    shape = eng.shape()  # the autotuned launch shapes (exact form)
 
     def barrier():
         if dist:
@@ -477,7 +478,7 @@ def run_ours(args):
         "config": {"workload": args.workload, "description": w["desc"], "n_site": n, "n_tet": len(P.tets),
                    "site_k": K, "tet_k": pkg.tet_k(n, len(P.tets)), "grid_dim": grid_dim, "method": args.method,
                    "knn_tiers": ([32, K] if exact and args.method == "cell_tet" and K > 32 else [K]),
-                   "robust_predicates": bool(args.robust_predicates),
+                   "robust_predicates": bool(args.robust_predicates), "launch_shape": shape,
                    "form": "exact (inside cells whole, boundary cells against every tet in reach)" if exact
                            else "reference (per-tet sums over tet_k candidates)",
                    "moments": "f32 atomics" if args.method == "plain" else "compensated f32 per site, f64 out",
@@ -529,13 +530,14 @@ def other_forms(pkg, P, K, value, args):
     out["chosen_over_reference_form"] = round(value / ref["value"], 2)
     # the precision configuration: Gaussian-mixture sites, same mesh and form
     Pg = make_problem("torus128_gaussian_1m")
-    with pkg.Engine(Pg.verts, Pg.tets, Pg.sites, site_k=K, use_graph=True, exact=True) as e:
+    with pkg.Engine(Pg.verts, Pg.tets, Pg.sites, site_k=K, use_graph=True, exact=True, autotune=True) as e:
         e.time_iterate(args.warmup, update=True)
         start = e.sites_original()
         ms = e.time_iterate(args.steps, update=True)
         prec = {"workload": "torus128_gaussian_1m", "description": WORKLOADS["torus128_gaussian_1m"]["desc"],
                 "value": round(args.steps / (ms / 1e3), 3), "ms_per_step": round(ms / args.steps, 4),
-                "steps": args.steps, "warmup": args.warmup, "site_k": e.site_k}
+                "steps": args.steps, "warmup": args.warmup, "site_k": e.site_k, "launch_shape": e.shape(),
+                "stats": e.stats()}
         e.set_sites(start)
         prec["accuracy"] = accuracy_pass(pkg, e, Pg, start)
     prec["over_plain"] = round(prec["value"] / plain["value"], 2)
@@ -545,7 +547,7 @@ def other_forms(pkg, P, K, value, args):
         out["batched_form"] = batch_measure(pkg, 3, 10, 0)
     # the small configuration, timed in full by the reference arm too
     Ps = make_problem("kuhn20_20k")
-    small = time_engine(pkg, Ps, 64, 5, 50, exact=True)
+    small = time_engine(pkg, Ps, 64, 5, 50, exact=True, autotune=True)
     small.update(workload="kuhn20_20k", description=WORKLOADS["kuhn20_20k"]["desc"])
     small.pop("stats")
     out["small_config"] = small
@@ -653,6 +655,7 @@ def batch_measure(pkg, warmup, steps, device):
                "n_prob": B.n_prob, "n_site": B.n_site, "n_tet": B.n_tet,
                "sites_per_s": round(B.n_site * steps / (ms / 1e3), 1),
                "site_k_histogram": {str(k): v for k, v in sorted(ks.items())}, "grid_density": round(B.density, 2),
+               "launch_shape": B.shape(),
                "generate_s": round(gen_s, 1), "create_s": round(create_s, 1)}
     return out
 

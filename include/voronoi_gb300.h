@@ -106,6 +106,8 @@ enum vgb_buffer {
                                   neighbour's distance, so it was clipped by every site
                                   within twice their radius (exact where it meets the mesh) */
 #define VGB_SITE_UNRESOLVED 64 /* a site beyond the K nearest may still cut the cell      */
+#define VGB_SITE_SCAN_FAILED 128 /* with UNRESOLVED: the completion's search itself gave up
+                                    (a degenerate cut, or no free plane slot)              */
 
 typedef struct vgb_config {
   int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9);
@@ -129,12 +131,19 @@ typedef struct vgb_config {
                    which gives up on such a cell, with the exact fallback it lacks.
                    Makes degenerate inputs (sites on a regular lattice, cospherical
                    neighbours) come out whole.                                      */
+  int autotune; /* exact cell-tet form.  1: at creation, time the launch shapes on the
+                   initial sites and keep the fastest -- warps per kNN block (4 or 8),
+                   lanes per site in the first clip pass (8 or 16) and vertices per
+                   cell in the one-warp clip pass (64 or 96); results do not depend on
+                   them beyond float rounding.  0: the defaults (8, 8, 64).  The
+                   batched form tunes them with the grid density (grid_dim 0).       */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;
 
 /* Defaults: site_k 90, tet_k 0, grid_dim 0, cell-tet, graphs on, device 0,
- * exact 0 (the reference's per-tet sums over tet_k candidates), robust_predicates 0. */
+ * exact 0 (the reference's per-tet sums over tet_k candidates), robust_predicates 0,
+ * autotune 0. */
 void vgb_config_init(vgb_config* cfg);
 
 /* One-line description of a CUDA device (name, SMs, memory) into buf. */
@@ -200,6 +209,11 @@ void vgb_host_free(void* p);
 /* Sizes the engine settled on. */
 int vgb_engine_info(vgb_engine* e, int* n_site, int* n_tet, int* site_k, int* tet_k, int* grid_dim);
 
+/* Launch shapes in use (autotuned with cfg.autotune): warps per kNN block,
+ * lanes per site in the first clip pass, triangle slots per lane of the
+ * one-warp clip pass (32 x slots vertices).  Any pointer may be NULL. */
+int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots);
+
 /* Device time in ms of the phases of the last non-graph pass:
  * [0] grid sort, [1] site kNN, [2] tet candidates, [3] site-major candidate
  * lists, [4] clip, [5] moments + update. */
@@ -262,6 +276,8 @@ int vgb_batch_sync(vgb_batch* b);
 /* n_iter iterations timed with CUDA events on the batch's stream. */
 int vgb_batch_time_iterate(vgb_batch* b, int n_iter, int update, float* ms);
 int vgb_batch_info(const vgb_batch* b, int* n_prob, int* n_site_total, int* n_tet_total, float* density);
+/* Launch shapes the batch's autotuner kept (as vgb_engine_shape). */
+int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots);
 /* Sizes and the tuned parameters of problem p. */
 int vgb_batch_problem(const vgb_batch* b, int p, int* n_site, int* n_tet, int* site_k, int* grid_dim,
                       int* field_dim);

@@ -114,3 +114,33 @@ def test_lone_engine_autotunes_k(pkg, meshgen):
             assert E.stats()["security_miss"] == 0
     with pkg.Batch([(P.verts, P.tets, P.sites)], site_k=0, tune_grid=False) as B:
         assert B.problem(0)["site_k"] == K
+
+
+def test_autotuned_shapes_give_the_same_cells(pkg, meshgen, oracle):
+    """The autotuner's launch shapes (kNN warps per block, first-pass lanes
+    per site, one-warp pass capacity) change how the work is laid out, not
+    the cells: the autotuned engine agrees with the default one to float
+    rounding, and the batch's tuned shape is one of the built ones."""
+    P = meshgen.cube_problem(10, 4000, seed=11, jitter=0.1)
+    runs = []
+    for tune in (False, True):
+        with pkg.Engine(P.verts, P.tets, P.sites, site_k=64, exact=True, autotune=tune) as E:
+            shape = E.shape()
+            E.iterate(1, update=False)
+            E.sync()
+            vol_g, _ = E.moments()
+            _, ids = E.sites()
+            vol = np.empty_like(vol_g)
+            vol[ids] = vol_g
+            runs.append((shape, vol))
+    (s0, v0), (s1, v1) = runs
+    assert s0 == {"knn_warps": 8, "build_lanes": 8, "fast_vertices": 64}
+    assert s1["knn_warps"] in (4, 8) and s1["build_lanes"] in (8, 16) and s1["fast_vertices"] in (64, 96)
+    big = v0 > 1e-9 * v0.max()
+    assert (np.abs(v1[big] - v0[big]) / v0[big]).max() < 1e-5
+    mv = oracle.mesh_volume(P.verts, P.tets)
+    assert abs(v1.sum() - mv) / mv < 1e-6
+    probs = _problems(meshgen)[:3]
+    with pkg.Batch([(Q.verts, Q.tets, Q.sites) for Q in probs], site_k=0, tune_grid=True) as B:
+        bs = B.shape()
+    assert bs["knn_warps"] in (4, 8) and bs["build_lanes"] in (8, 16) and bs["fast_vertices"] in (64, 96)
