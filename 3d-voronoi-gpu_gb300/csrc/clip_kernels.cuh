@@ -142,6 +142,9 @@ struct SiteSmem {
   // neighbours missed the security radius; in the completion pass, the
   // bound its earlier pass left
   float pr2;
+  // completion pass: no site beyond the K nearest cut the cell, so the
+  // earlier pass's moments are exact and stand
+  int unchanged;
 };
 
 // Compensated add (TwoSum) of x into the pair (hi, lo) in shared memory.
@@ -319,6 +322,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     if (lane == 0) {
       S.site_flags = SITE_HANDED | (SL > 2 ? SITE_REDO : 0);
       S.pr2 = COMPLETE ? esc_r2[it] : 0.f;
+      S.unchanged = 0;
       S.Rc = 0.f;
       S.nfaces = 0;
       S.seg = -1;
@@ -663,7 +667,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
           const int cj = grid_axis(seed.y, dim), ck = grid_axis(seed.z, dim);
           const int rmax = max(max(cj - j0, j1 - cj), max(ck - k0, k1 - ck));
           const int first_free = 4 + K + 2 * BOX_PLANES;  // slots below: the site's own planes
-          int nxt = first_free;
+          int nxt = first_free, ncut = 0;
           bool fail = state != 0;
           // the far vertices of the current cell into S.mv[0, nfar)
           auto gather_far = [&]() {
@@ -715,6 +719,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
                     const int r = warp_clip<SL, ROBUST>(c, Q, (unsigned)nxt, S.plane, S.conf, S.bedge, lane, true,
                                                         S.cnt + WC_NEWV, S.cnt + WC_EXACT);
                     if (r == CLIP_CUT) {
+                      ++ncut;
                       // the lowest free slot: no live vertex refers to it
                       unsigned used[PWORDS];
 #pragma unroll
@@ -748,6 +753,16 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
                 }
               }
           cdone = !fail;
+          if (cdone && ncut == 0) {
+            // nothing beyond the K nearest cuts the cell: the earlier pass's
+            // pieces were exact; keep them and clip no tet again
+            if (lane == 0) {
+              S.site_flags |= SITE_COMPLETED | (secmiss ? SITE_SECMISS : 0);
+              S.unchanged = 1;
+            }
+            __syncwarp();
+            break;
+          }
           if (!cdone && lane == 0) S.site_flags |= SITE_SCAN_FAILED;
         }
         const bool miss_left = secmiss && !cdone;
@@ -895,7 +910,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     if (lane == 0) {
       unsigned f = S.site_flags;
       // a completion that failed keeps the earlier pass's moments
-      const bool keep_old = COMPLETE && (f & (SITE_UNRESOLVED | SITE_DROPPED));
+      const bool keep_old = COMPLETE && ((f & (SITE_UNRESOLVED | SITE_DROPPED)) || S.unchanged);
       if (!keep_old)
         mom[s] = make_dmom4((double)S.acc[0] + (double)S.acc[4], (double)S.acc[1] + (double)S.acc[5],
                             (double)S.acc[2] + (double)S.acc[6], (double)S.acc[3] + (double)S.acc[7]);
@@ -918,7 +933,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
           S.cnt[WC_SECMISS]++;
           if (prob_secmiss) atomicAdd(prob_secmiss + pidx, 1u);
         }
-        if (COMPLETE) S.cnt[keep_old ? WC_UNRESOLVED : WC_COMPLETED]++;
+        if (COMPLETE) S.cnt[(f & (SITE_UNRESOLVED | SITE_DROPPED)) ? WC_UNRESOLVED : WC_COMPLETED]++;
       }
     }
     __syncwarp();

@@ -205,13 +205,15 @@ def measured_peaks():
     return 6800.0, 2070.0, "fallback"
 
 
-# DRAM traffic per launch of the rooflined kernels, from ncu captures of the
-# 125,000-site torus workload (64^3 grid: one kernel, one launch, 1 pass of
-# dram__bytes_read.sum + dram__bytes_write.sum) scaled to the 1M-site
-# workload by its site count, and the capture it came from.  Both kernels
-# move bytes in proportion to the sites (rows of neighbours, site records,
-# tet records of the handed-on cells).
-TRAFFIC = {}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# the rooflined kernels on the default workload, from one-pass ncu captures
+# of one launch each: the clip phase's two large kernels (first pass
+# 253.5 MB, one-warp pass 502.1 MB) and the first kNN tier (93.1 MB).
+TRAFFIC = {
+    ("clip", "torus128_uniform_1m"): (755_616_512, "ncu one-pass capture, k_build<0,8,4,0> + "
+                                                  "k_clip_site<1,0,2,0,0>, one launch each"),
+    ("knn", "torus128_uniform_1m"): (93_052_672, "ncu one-pass capture, k_knn<1,0,8>, one launch"),
+}
 
 
 # ---------------------------------------------------------------------------
