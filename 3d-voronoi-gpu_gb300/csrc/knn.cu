@@ -156,6 +156,46 @@ __device__ __forceinline__ void warp_merge(u64 (&L)[S], u64 b, int lane) {
   L[0] = c;
 }
 
+// Take cnt (<= 32) buffered keys into the list.  While the list is empty
+// the buffer only needs sorting; a few keys are inserted one by one -- a
+// ballot per slot gives the insertion point in the sorted list, shuffles move
+// the larger keys up by one entry -- which costs less than the sort and merge
+// networks; otherwise the bitonic merge.  Keys are distinct (the id is in the low
+// bits), so each way gives the same list.
+constexpr int KNN_INSERT_MAX = 8;
+
+template <int S>
+__device__ __forceinline__ void warp_absorb(u64 (&L)[S], const u64* buf, int cnt, int filled, int lane) {
+  if (filled == 0) {
+    L[0] = warp_sort32(lane < cnt ? buf[lane] : KEY_NONE, lane);
+    return;
+  }
+  if (cnt * S <= KNN_INSERT_MAX) {
+    for (int c = 0; c < cnt; ++c) {
+      const u64 k = buf[c];
+      // insertion point: keys below k, over every slot (entry s * 32 + lane)
+      int pos = 0;
+#pragma unroll
+      for (int q = 0; q < S; ++q) pos += __popc(__ballot_sync(KFULL, L[q] < k));
+      // every entry at or past pos takes its predecessor's key
+      u64 prev[S];
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const u64 up = __shfl_up_sync(KFULL, L[q], 1);
+        const u64 wrap = q > 0 ? __shfl_sync(KFULL, L[q > 0 ? q - 1 : 0], 31) : KEY_NONE;
+        prev[q] = lane > 0 ? up : wrap;
+      }
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const int e = q * 32 + lane;
+        if (e >= pos) L[q] = e == pos ? k : prev[q];
+      }
+    }
+    return;
+  }
+  warp_merge<S>(L, lane < cnt ? buf[lane] : KEY_NONE, lane);
+}
+
 template <int S>
 __device__ __forceinline__ u64 kth_key(const u64 (&L)[S], int K) {
   const int s = (K - 1) >> 5;
@@ -305,8 +345,9 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
             __syncwarp();
             if (lane + 32 < cnt) buf[lane] = rest;
             cnt -= 32;
+            if (filled == 0) L[0] = warp_sort32(b, lane);  // nothing to merge with yet
+            else warp_merge<S>(L, b, lane);
             filled += 32;
-            warp_merge<S>(L, b, lane);
             tau = kth_key<S>(L, K);
             __syncwarp();
           }
@@ -315,18 +356,16 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
       // flush once the list can hold K keys (the stop test needs the k-th)
       if (cnt > 0 && filled + cnt >= K) {
         __syncwarp();
-        const u64 b = lane < cnt ? buf[lane] : KEY_NONE;
+        warp_absorb<S>(L, buf, cnt, filled, lane);
         filled += cnt;
         cnt = 0;
-        warp_merge<S>(L, b, lane);
         tau = kth_key<S>(L, K);
         __syncwarp();
       }
     }
     if (cnt > 0) {
       __syncwarp();
-      const u64 b = lane < cnt ? buf[lane] : KEY_NONE;
-      warp_merge<S>(L, b, lane);
+      warp_absorb<S>(L, buf, cnt, filled, lane);
       __syncwarp();
     }
     unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * Kr : out + P.knn_off + (size_t)(qs - P.site_off) * Kr;
