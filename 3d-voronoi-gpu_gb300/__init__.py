@@ -58,7 +58,7 @@ def build(force: bool = False) -> Path:
 class _Config(C.Structure):
     _fields_ = [("site_k", C.c_int), ("tet_k", C.c_int), ("grid_dim", C.c_int), ("method", C.c_int),
                 ("use_graph", C.c_int), ("device", C.c_int), ("exact", C.c_int), ("robust_predicates", C.c_int),
-                ("autotune", C.c_int)]
+                ("autotune", C.c_int), ("tet_pieces", C.c_int)]
 
 
 class _KnProblem(C.Structure):
@@ -105,8 +105,8 @@ def lib() -> C.CDLL:
     L.vgb_engine_phase_ms.argtypes = [vp, C.POINTER(C.c_float)]
     L.vgb_engine_time_iterate.argtypes = [vp, i, i, C.POINTER(C.c_float)]
     L.vgb_engine_set_graph.argtypes = [vp, i]
-    L.vgb_engine_shape.argtypes = [vp, ip, ip, ip]
-    L.vgb_batch_shape.argtypes = [vp, ip, ip, ip]
+    L.vgb_engine_shape.argtypes = [vp, ip, ip, ip, ip]
+    L.vgb_batch_shape.argtypes = [vp, ip, ip, ip, ip]
     L.vgb_host_alloc.argtypes = [sz]
     L.vgb_host_alloc.restype = vp
     L.vgb_host_free.argtypes = [vp]
@@ -178,12 +178,15 @@ class Engine:
     robust_predicates=True: vertex-vs-plane tests within 1e-4 of zero (relative
     to their terms) are decided by exact determinant signs (the reference's
     arithmetic filter, with an exact fallback); degenerate inputs such as
-    lattice sites come out whole.
+    lattice sites come out whole.  tet_pieces=True (cell-tet): the pieces
+    cell ^ tet of the cells the first pass does not finish are built from
+    their tets, clipped by the cell faces crossing them; False (default)
+    clips a copy of the cell by each tet.
     """
 
     def __init__(self, verts, tets, sites, site_k: int = 90, tet_k: int = 0, grid_dim: int = 0,
                  method: str = "cell_tet", use_graph: bool = True, device: int = 0, exact: bool = False,
-                 robust_predicates: bool = False, autotune: bool = False):
+                 robust_predicates: bool = False, autotune: bool = False, tet_pieces: bool = False):
         L = lib()
         self._verts = _f32(verts)
         self._tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -197,6 +200,7 @@ class Engine:
         cfg.exact = int(exact)
         cfg.robust_predicates = int(robust_predicates)
         cfg.autotune = int(autotune)
+        cfg.tet_pieces = int(tet_pieces)
         h = C.c_void_p()
         _check(L.vgb_engine_create(C.byref(h), C.byref(cfg), _p(self._verts), len(self._verts), _p(self._tets),
                                    len(self._tets), _p(s), len(s)), "vgb_engine_create")
@@ -228,10 +232,11 @@ class Engine:
 
     def shape(self) -> dict:
         """Launch shapes in use: kNN warps per block, first-pass lanes per
-        site, one-warp pass vertex capacity."""
-        v = [C.c_int() for _ in range(3)]
+        site, one-warp pass vertex capacity, clip form (tet_pieces)."""
+        v = [C.c_int() for _ in range(4)]
         _check(lib().vgb_engine_shape(self._h, *[C.byref(x) for x in v]), "vgb_engine_shape")
-        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value}
+        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value,
+                "tet_pieces": v[3].value}
 
     def set_sites(self, sites):
         s = _f32(sites)
@@ -321,7 +326,7 @@ class Batch:
     """
 
     def __init__(self, problems, site_k: int = 0, tune_grid: bool = True, use_graph: bool = True,
-                 device: int = 0, robust_predicates: bool = False):
+                 device: int = 0, robust_predicates: bool = False, tet_pieces: bool = False):
         L = lib()
         self._v = [_f32(v) for v, _, _ in problems]
         self._t = [np.ascontiguousarray(t, dtype=np.int32) for _, t, _ in problems]
@@ -341,6 +346,7 @@ class Batch:
         cfg.site_k, cfg.grid_dim = site_k, 0 if tune_grid else 1
         cfg.method, cfg.use_graph, cfg.device, cfg.exact = METHODS["cell_tet"], int(use_graph), device, 1
         cfg.robust_predicates = int(robust_predicates)
+        cfg.tet_pieces = int(tet_pieces)
         h = C.c_void_p()
         _check(L.vgb_batch_create(C.byref(h), C.byref(cfg), P, vp_arr, nv, tp_arr, nt, sp_arr, ns),
                "vgb_batch_create")
@@ -368,9 +374,10 @@ class Batch:
 
     def shape(self) -> dict:
         """Launch shapes the autotuner kept (see Engine.shape)."""
-        v = [C.c_int() for _ in range(3)]
+        v = [C.c_int() for _ in range(4)]
         _check(lib().vgb_batch_shape(self._h, *[C.byref(x) for x in v]), "vgb_batch_shape")
-        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value}
+        return {"knn_warps": v[0].value, "build_lanes": v[1].value, "fast_vertices": 32 * v[2].value,
+                "tet_pieces": v[3].value}
 
     def problem(self, p: int) -> dict:
         """Sizes and tuned parameters of problem p."""

@@ -102,7 +102,8 @@ void free_batch(vgb_batch* b) {
   void* bufs[] = {b->d_probs, b->site_prob, b->tet_prob, b->verts, b->tets, b->sites, b->sites_tmp,
                   b->cell_start, b->cell_fill, b->site_cell, b->scan_tmp, b->pos_of_id, b->tet_order,
                   b->tet_cell_start, b->tcell, b->knn, b->mom, b->stats, b->field, b->field_sat, b->reach,
-                  b->tet_sph, b->reach_max, b->secmiss, b->redo_list, b->redo_count, b->store.tri, b->store.nt};
+                  b->tet_sph, b->reach_max, b->secmiss, b->redo_list, b->redo_count, b->store.tri, b->store.nt,
+                  b->store.faces};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->st) cudaStreamDestroy(b->st);
@@ -280,6 +281,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
   vgb_batch* b = new (std::nothrow) vgb_batch();
   if (!b) { set_error("host allocation failed"); return VGB_ERR_NOMEM; }
   b->cfg = cfg;
+  b->shape.pieces = cfg.tet_pieces ? 1 : 0;
   b->n_prob = n_prob;
   b->n = (int)ns_tot;
   b->n_tet = (int)nt_tot;
@@ -347,8 +349,9 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       (rc = balloc(&b->stats, VGB_STAT_COUNT)) || (rc = balloc(&b->field, f_off)) ||
       (rc = balloc(&b->field_sat, q_off)) || (rc = balloc(&b->reach, b->n_tet)) ||
       (rc = balloc(&b->tet_sph, b->n_tet)) || (rc = balloc(&b->reach_max, n_prob)) ||
-      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 5 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 12)) ||
-      (rc = balloc(&b->store.tri, (size_t)b->n * vgb::STORE_VERTS)) || (rc = balloc(&b->store.nt, b->n))) {
+      (rc = balloc(&b->secmiss, n_prob)) || (rc = balloc(&b->redo_list, 6 * (size_t)b->n)) || (rc = balloc(&b->redo_count, 12)) ||
+      (rc = balloc(&b->store.tri, (size_t)b->n * vgb::STORE_VERTS)) || (rc = balloc(&b->store.nt, b->n)) ||
+      (rc = balloc(&b->store.faces, (size_t)b->n * vgb::PIECE_REC))) {
     free_batch(b);
     return rc;
   }
@@ -460,9 +463,11 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     // the fastest with 4-warp kNN blocks
     static const int shapes[4][2] = {{8, 2}, {16, 2}, {8, 3}, {16, 3}};
     vgb::KernelShape bs{};
+    bs.pieces = b->cfg.tet_pieces ? 1 : 0;
     float bms = 1e30f;
     for (auto& sh : shapes) {
       vgb::KernelShape t{};
+      t.pieces = bs.pieces;
       t.build_g = sh[0];
       t.fast_sl = sh[1];
       b->shape = t;
@@ -521,11 +526,12 @@ int vgb_batch_time_iterate(vgb_batch* b, int n_iter, int update, float* ms) {
   return VGB_OK;
 }
 
-int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots) {
+int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots, int* tet_pieces) {
   if (!b) { set_error("NULL batch"); return VGB_ERR_INVALID; }
   if (knn_warps) *knn_warps = b->shape.knn_warps;
   if (build_lanes) *build_lanes = b->shape.build_g;
   if (fast_slots) *fast_slots = b->shape.fast_sl;
+  if (tet_pieces) *tet_pieces = b->shape.pieces;
   return VGB_OK;
 }
 

@@ -155,6 +155,33 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float x) {
   hi = s;
 }
 
+// Bisector plane of the site and a neighbour B in site-relative
+// coordinates: n = -b, w = |b|^2 / 2 (b = B - site).  Every pass makes it
+// with this one expression, so a plane id names the same bits everywhere.
+__device__ __forceinline__ float4 bisector_plane(float4 seed, float4 B) {
+  const float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
+  const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
+  return make_float4(-bx, -by, -bz, 0.5f * bb);
+}
+
+// The reference's box [-0.1, 1000.1]^3 (voronoi.cu:125-161) and the half
+// side of the cube centred on a site that contains it.
+constexpr float DOMAIN_LO = -0.1f, DOMAIN_HI = 1000.1f;
+__device__ __forceinline__ float cube_half_side(float4 p) {
+  return fmaxf(fmaxf(fmaxf(p.x - DOMAIN_LO, DOMAIN_HI - p.x), fmaxf(p.y - DOMAIN_LO, DOMAIN_HI - p.y)),
+               fmaxf(p.z - DOMAIN_LO, DOMAIN_HI - p.z)) + 1.f;
+}
+// Start plane b of a site (site-relative): 0-5 the faces of the cube of half
+// side L centred on it (+x, -x, +y, -y, +z, -z bounds in turn), 6-11 the
+// domain box's faces in the same order.
+__device__ __forceinline__ float4 start_plane(int b, float4 seed, float L) {
+  const int c = b < BOX_PLANES ? b : b - BOX_PLANES, ax = c >> 1;
+  const float sgn = (c & 1) ? -1.f : 1.f;
+  const float sc = ax == 0 ? seed.x : ax == 1 ? seed.y : seed.z;
+  const float w = b < BOX_PLANES ? L : (c & 1) ? DOMAIN_HI - sc : sc - DOMAIN_LO;
+  return make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, w);
+}
+
 // Bounding box of the cell's vertices (site-relative), over the warp: float
 // bits mapped to an order-preserving unsigned key for the integer reductions.
 __device__ __forceinline__ unsigned ord_key(float f) {
@@ -236,7 +263,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ out_list,
     int* __restrict__ out_count, int* __restrict__ work, const CellStore store, int k_tier,
     const int* __restrict__ cell_start, int* __restrict__ esc_list, float* __restrict__ esc_r2,
-    int* __restrict__ esc_count) {
+    int* __restrict__ esc_count, int* __restrict__ piece_list, int* __restrict__ piece_count) {
   constexpr int NPLANE = COMPLETE ? COMPLETE_PLANES : SITE_PLANES;
   constexpr int PWORDS = (NPLANE + 31) / 32;
   __shared__ SiteSmem<SL, NPLANE> smem_all[CLIP_WARPS];
@@ -265,6 +292,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
   for (int it = work ? next_item(0) : blockIdx.x * CLIP_WARPS + wib; it < n_items; it = next_item(it)) {
     const int s = in_list ? in_list[it] : it;
     bool abandon = false;
+    bool emitted = false;  // handed to the pieces pass
     // the cell the first pass built, when it stored one
     if (lane == 0) S.stored = (CELL_TET && store.nt) ? store.nt[s] : 0;
     __syncwarp();
@@ -281,12 +309,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     const int Kload = (stored_secure && k_tier > 0 && k_tier < K) ? k_tier : K;
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
-    for (int j = lane; j < Kload; j += WARP) {
-      float4 B = sites[krow[j]];
-      float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
-      float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
-      S.plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
-    }
+    for (int j = lane; j < Kload; j += WARP) S.plane[4 + j] = bisector_plane(seed, sites[krow[j]]);
     // The reference starts the cell-tet cell from the box [-0.1, 1000.1]^3
     // (voronoi.cu:125-161).  Here it starts from a cube centred on the site
     // that contains that box: every tet lies inside both, so the cell clipped
@@ -296,25 +319,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     // The reference's box itself (planes 4+K+6..) bounds the part of the
     // cell that can meet a tet: it gives the security radius and the culling
     // radius, while the cube-start cell is what the tets clip.
-    constexpr float lo = -0.1f, hi = 1000.1f;
-    auto cube_half = [&](float4 p) {
-      return fmaxf(fmaxf(fmaxf(p.x - lo, hi - p.x), fmaxf(p.y - lo, hi - p.y)), fmaxf(p.z - lo, hi - p.z)) + 1.f;
-    };
     if (lane == 0) S.seed = seed;
-    if (CELL_TET) {
-      const float L = cube_half(seed);
-      if (lane < BOX_PLANES) {
-        const int ax = lane >> 1;
-        const float sgn = (lane & 1) ? -1.f : 1.f;
-        S.plane[4 + K + lane] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
-      } else if (lane < 2 * BOX_PLANES) {
-        const int b = lane - BOX_PLANES, ax = b >> 1;
-        const float sgn = (b & 1) ? -1.f : 1.f;
-        const float sc = ax == 0 ? seed.x : ax == 1 ? seed.y : seed.z;
-        S.plane[4 + K + lane] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f,
-                                            (b & 1) ? hi - sc : sc - lo);
-      }
-    }
+    if (CELL_TET && lane < 2 * BOX_PLANES) S.plane[4 + K + lane] = start_plane(lane, seed, cube_half_side(seed));
     __syncwarp();
 
     if (lane < 8) S.acc[lane] = 0.f;  // site-relative volume and first moment
@@ -370,7 +376,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
         c.nt = nt0;
         c.r2 = warp_max_nonneg(lm);
       } else if (job == 0) {
-        const float L = cube_half(S.seed);
+        const float L = cube_half_side(S.seed);
         if (lane < 8) {
           // corner (bx, by, bz) of the cube: faces 4+K+{0|1}, +{2|3}, +{4|5},
           // ordered so each dual triangle has a negative normal determinant
@@ -820,7 +826,6 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
         if (interior && lane == 0) S.site_flags |= SITE_INTERIOR;
         if (COMPLETE && lane == 0) S.site_flags |= cdone ? SITE_COMPLETED : SITE_UNRESOLVED;
         if (!interior) {
-          if (!build_miss || COMPLETE) store_master(c, S, lane);
           // the planes that bound the cell (ids present in its triangles)
           // (a bit per plane id, five words; selected by comparison so the
           // words stay in registers)
@@ -846,12 +851,32 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
             nfaces += __popc(hm);
           }
           if (lane == 0) S.nfaces = nfaces;
+          __syncwarp();
+          // With the pieces pass, the cell's record (face ids, radius,
+          // outcome so far) goes to it and the site is done here; the
+          // pieces pass clips each candidate tet by the faces crossing it.
+          emitted = CELL_TET && !COMPLETE && piece_list != nullptr && nfaces <= PIECE_FACES;
+          if (emitted) {
+            unsigned* const rec = store.faces + (size_t)s * PIECE_REC;
+            if (lane < PIECE_FACES / 4)
+              rec[4 + lane] = (unsigned)S.faces[4 * lane] | ((unsigned)S.faces[4 * lane + 1] << 8) |
+                              ((unsigned)S.faces[4 * lane + 2] << 16) | ((unsigned)S.faces[4 * lane + 3] << 24);
+            if (lane == 0) {
+              rec[0] = (unsigned)nfaces;
+              rec[1] = __float_as_uint(Rc);
+              rec[2] = S.site_flags;
+              rec[3] = 0u;
+              piece_list[atomicAdd(piece_count, 1)] = s;
+            }
+          } else if (!build_miss || COMPLETE) {
+            store_master(c, S, lane);
+          }
           // candidate tets: the site's candidate list (the reference's tet_k
           // sets), or, in the exact form, the x-runs of centroid-grid cells
           // within reach of the cell -- a tet meeting the cell has its
           // centroid within Rc + rt_max of the site, and no tet reaches
           // farther than the largest reach
-          if (lane == 0) {
+          if (lane == 0 && !emitted) {
             if (exact) {
               const int dim = PD(dim);
               const float R =
@@ -895,7 +920,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
         S.cnt[WC_EMPTY]++;
       }
       __syncwarp();
-      if (interior) break;
+      if (interior || emitted) break;
     }
     if (abandon) {
       // the larger-capacity pass redoes this site from scratch
@@ -907,6 +932,7 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
       __syncwarp();
       continue;
     }
+    if (emitted) continue;  // the pieces pass finishes the site
     if (lane == 0) {
       unsigned f = S.site_flags;
       // a completion that failed keeps the earlier pass's moments
@@ -939,6 +965,400 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
     __syncwarp();
 #undef PD
   }
+  if (stats && lane < WC_N && S.cnt[lane]) atomicAdd(stats + stat_slot(lane), (unsigned long long)S.cnt[lane]);
+}
+
+// ---------------------------------------------------------------------------
+// Pieces pass of the cell-tet method.  For the sites the one-warp pass hands
+// on (their cell records in CellStore::faces), each piece cell ^ tet is
+// built from the tet: its four corners, clipped by the cell faces that cross
+// it (the piece is the tet cut by the half-spaces of the cell's faces; a face
+// with all four corners on its inside cannot cut it, one with all four
+// outside culls the tet).  A lane group of 8 lanes x 4 triangle slots (32
+// vertices) holds a piece, four tets per warp on one instruction stream
+// (group_clip).  A piece has about a quarter of the cell's vertices, so its
+// cuts remove small cavities where a copy of the cell loses about half of
+// its vertices to each tet face.
+//
+// One warp per site: its face planes (from the record's plane ids, computed
+// as the one-warp pass computed them), the candidate scan of k_clip_site
+// (the same tests), each survivor queued with the mask of the faces crossing
+// it, then the queue four pieces at a time; the pieces' moments go into the
+// site's compensated sums in queue order.  A piece that outgrows 32 vertices
+// sends the site to the 128-vertex pass (out_list), which redoes it with
+// copies of the cell.
+// ---------------------------------------------------------------------------
+constexpr int PIECE_G = 8, PIECE_SL = 4, PIECE_NG = WARP / PIECE_G;
+constexpr int PIECE_TET0 = PIECE_FACES;  // the groups' tet faces: plane ids PIECE_TET0 + 4 g + i
+// The queue is refilled a chunk of 32 candidates at a time while it holds
+// less than a round of pieces (one per group).
+constexpr int PIECE_QUEUE = WARP + PIECE_NG;
+#ifndef VGB_PIECE_MIN_BLOCKS
+#define VGB_PIECE_MIN_BLOCKS 8
+#endif
+
+struct PieceSmem {
+  float4 plane[PIECE_FACES + 4 * PIECE_NG];    // the cell's faces, then each group's tet faces
+  unsigned conf[PIECE_NG][PIECE_G * PIECE_SL];   // clip scratch of each group
+  unsigned bedge[PIECE_NG][PIECE_G * PIECE_SL];
+  unsigned queue[PIECE_QUEUE];                   // surviving candidate tets, in scan order
+  unsigned qmask[2][PIECE_QUEUE];                // the faces crossing each (bits 0-31, 32-63)
+  float4 corner[PIECE_NG][4];                    // corners of each group's tet
+  unsigned fid[PIECE_FACES / 4];                 // the record's face ids, four per word
+  unsigned cnt[WC_N];                            // per-warp counters (lane 0 writes)
+  unsigned gnew[PIECE_NG];                       // new vertices, per group
+  float acc[8];                                  // compensated sums: hi parts 0-3, lo parts 4-7
+  int scan[6];                                   // candidate rows, as SiteSmem::scan
+  int seg, base, se;                             // the scan's position, as SiteSmem
+  float Rc, pr2;
+  unsigned site_flags;
+  float4 seed;
+};
+
+template <bool BATCHED, bool ROBUST>
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_PIECE_MIN_BLOCKS) k_clip_pieces(
+    const float4* __restrict__ sites, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
+    const int* __restrict__ site_prob, const ProbDesc lone, const float4* __restrict__ verts,
+    const int4* __restrict__ tets, const int* __restrict__ site_start, const int* __restrict__ site_tets,
+    dmom4* __restrict__ mom, unsigned long long* __restrict__ stats, const int* __restrict__ tet_order,
+    const int* __restrict__ tet_cell_start, const float4* __restrict__ tet_sph, const float* __restrict__ reach,
+    const unsigned* __restrict__ reach_max_bits, unsigned* __restrict__ prob_secmiss,
+    const int* __restrict__ in_list, const int* __restrict__ in_count, int* __restrict__ work,
+    int* __restrict__ out_list, int* __restrict__ out_count, const CellStore store, int* __restrict__ esc_list,
+    float* __restrict__ esc_r2, int* __restrict__ esc_count) {
+  __shared__ PieceSmem smem_all[CLIP_WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gid = lane / PIECE_G, gl = lane % PIECE_G, gbase = gid * PIECE_G;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  PieceSmem& S = smem_all[wib];
+  const bool exact = tet_order != nullptr;
+  if (lane < WC_N) S.cnt[lane] = 0u;
+  if (lane < PIECE_NG) S.gnew[lane] = 0u;
+  __syncwarp();
+  const int n_items = *in_count;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(work, 1);
+    it = __shfl_sync(FULL, it, 0);
+    if (it >= n_items) break;
+    const int s = in_list[it];
+    const int pidx = BATCHED ? site_prob[s] : 0;
+#define PD(f) (BATCHED ? probs[pidx].f : lone.f)
+    int nfaces;
+    {
+      // the record, then the face planes as the one-warp pass made them
+      const unsigned* const rec = store.faces + (size_t)s * PIECE_REC;
+      const unsigned w = lane < PIECE_REC ? rec[lane] : 0u;
+      nfaces = (int)__shfl_sync(FULL, w, 0);
+      const float Rc = __uint_as_float(__shfl_sync(FULL, w, 1));
+      const float4 seed = sites[s];
+      if (lane >= 4 && lane < PIECE_REC) S.fid[lane - 4] = w;
+      const unsigned flags0 = __shfl_sync(FULL, w, 2);
+      if (lane == 0) {
+        S.seed = seed;
+        S.Rc = Rc;
+        S.site_flags = flags0;
+        S.pr2 = 0.f;
+        S.seg = -1;
+        S.base = 0;
+        S.se = 0;
+      }
+      if (lane < 8) S.acc[lane] = 0.f;
+      __syncwarp();
+      const int K = PD(K);
+      const unsigned* const krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
+      const float L = cube_half_side(seed);
+      for (int f = lane; f < nfaces; f += WARP) {
+        const int id = (int)((S.fid[f >> 2] >> (8 * (f & 3))) & 0xffu);
+        S.plane[f] = id < 4 + K ? bisector_plane(seed, sites[krow[max(id - 4, 0)]]) : start_plane(id - 4 - K, seed, L);
+      }
+      if (lane == 0) {
+        if (exact) {
+          const int dim = PD(dim);
+          const float R = fminf(__fmaf_rn(PD(rt_max), 1.001f, Rc), __uint_as_float(reach_max_bits[pidx])) + 0.01f;
+          const int j0 = grid_axis(seed.y - R, dim), k0 = grid_axis(seed.z - R, dim);
+          const int nj = grid_axis(seed.y + R, dim) - j0 + 1;
+          S.scan[0] = nj * (grid_axis(seed.z + R, dim) - k0 + 1);
+          S.scan[1] = nj;
+          S.scan[2] = grid_axis(seed.x - R, dim);
+          S.scan[3] = grid_axis(seed.x + R, dim);
+          S.scan[4] = j0;
+          S.scan[5] = k0;
+        } else {
+          S.scan[0] = 1;
+        }
+      }
+      __syncwarp();
+    }
+
+    bool abandon = false, scan_done = false;
+    int nq = 0;  // queued survivors (warp-uniform)
+    while (!abandon) {
+      // ---------------------------------------------------------------
+      // fill the queue to a round of pieces, 32 candidates at a time (one
+      // per lane), or to the end of the scan
+      while (nq < PIECE_NG) {
+        const int base = S.base, se = S.se;
+        if (base >= se) {
+          const int seg = S.seg + 1;
+          __syncwarp();
+          if (seg >= S.scan[0]) {
+            scan_done = true;
+            break;
+          }
+          int b0, b1;
+          if (exact) {
+            const int pd = PD(dim), nj = S.scan[1];
+            const int row = PD(cell_off) + pd * ((S.scan[4] + seg % nj) + pd * (S.scan[5] + seg / nj));
+            b0 = tet_cell_start[S.scan[2] + row];
+            b1 = tet_cell_start[S.scan[3] + row + 1];
+          } else {
+            b0 = site_start[s];
+            b1 = site_start[s + 1];
+          }
+          if (lane == 0) {
+            S.seg = seg;
+            S.base = b0;
+            S.se = b1;
+          }
+          __syncwarp();
+          continue;
+        }
+        const int idx = base + lane;
+        const bool valid = idx < se;
+        const float Rc = S.Rc;
+        const float4 seed = S.seed;
+        unsigned cull_lane = 0;
+        int t = -1;
+        float3 v0 = make_float3(0.f, 0.f, 0.f), v1 = v0, v2 = v0, v3 = v0;
+        bool alive = valid;
+        if (exact && valid) {
+          // bounding spheres, and the tet's reach (as k_clip_site)
+          const float4 sp = tet_sph[idx];
+          const float ex = sp.x - seed.x, ey = sp.y - seed.y, ez = sp.z - seed.z;
+          const float dm = sqrtf(dot3_rn(ex, ey, ez, ex, ey, ez));
+          alive = dm <= __fmaf_rn(Rc + sp.w, 1.0001f, 1e-3f) && dm <= __fmaf_rn(reach[idx], 1.0001f, 1e-2f);
+        }
+        if (alive) {
+          t = exact ? tet_order[idx] : site_tets[idx];
+          const int4 q = tets[t];
+          const float4 a = verts[q.x], b = verts[q.y], cc = verts[q.z], d = verts[q.w];
+          v0 = make_float3(a.x - seed.x, a.y - seed.y, a.z - seed.z);
+          v1 = make_float3(b.x - seed.x, b.y - seed.y, b.z - seed.z);
+          v2 = make_float3(cc.x - seed.x, cc.y - seed.y, cc.z - seed.z);
+          v3 = make_float3(d.x - seed.x, d.y - seed.y, d.z - seed.z);
+          if (!exact) {
+            // bounding spheres: the cell lies within Rc of the site
+            const float mx = 0.25f * (v0.x + v1.x + v2.x + v3.x), my = 0.25f * (v0.y + v1.y + v2.y + v3.y),
+                        mz = 0.25f * (v0.z + v1.z + v2.z + v3.z);
+            auto d2 = [&](float3 v) { return dot3_rn(v.x - mx, v.y - my, v.z - mz, v.x - mx, v.y - my, v.z - mz); };
+            const float rt2 = fmaxf(fmaxf(d2(v0), d2(v1)), fmaxf(d2(v2), d2(v3)));
+            const float dm = sqrtf(dot3_rn(mx, my, mz, mx, my, mz));
+            if (dm > __fmaf_rn(Rc + sqrtf(rt2), 1.0001f, 1e-3f)) alive = false;
+          }
+        }
+        // each face of the cell: all four corners strictly outside culls the
+        // tet, some outside makes it a face the piece is clipped by
+        unsigned m0 = 0u, m1 = 0u;
+        for (int f = 0; f < nfaces; ++f) {
+          if (!__any_sync(FULL, alive)) break;
+          const float4 P = S.plane[f];
+          if (alive) {
+            ++cull_lane;
+            const bool o0 = plane_eval(P, v0.x, v0.y, v0.z) < 0.f, o1 = plane_eval(P, v1.x, v1.y, v1.z) < 0.f;
+            const bool o2 = plane_eval(P, v2.x, v2.y, v2.z) < 0.f, o3 = plane_eval(P, v3.x, v3.y, v3.z) < 0.f;
+            if (o0 && o1 && o2 && o3) {
+              alive = false;
+            } else if (o0 || o1 || o2 || o3) {
+              if (f < 32) m0 |= 1u << f;
+              else m1 |= 1u << (f - 32);
+            }
+          }
+        }
+        const unsigned survivors = __ballot_sync(FULL, alive);
+        const int nvalid = min(WARP, se - base);
+        const int nsurv = __popc(survivors);
+        if (alive) {
+          const int qp = nq + __popc(survivors & lt_mask);
+          S.queue[qp] = (unsigned)t;
+          S.qmask[0][qp] = m0;
+          S.qmask[1][qp] = m1;
+        }
+        nq += nsurv;
+        const unsigned cull_warp = __reduce_add_sync(FULL, cull_lane);
+        __syncwarp();
+        if (lane == 0) {
+          S.cnt[WC_CAND] += (unsigned)nvalid;
+          S.cnt[WC_CULLED] += (unsigned)(nvalid - nsurv);
+          S.cnt[WC_CLIPPED] += (unsigned)nsurv;
+          S.cnt[WC_CULLTESTS] += cull_warp;
+          S.base = base + WARP;
+        }
+        __syncwarp();
+      }
+      if (nq == 0) break;  // no candidate left
+
+      // ---------------------------------------------------------------
+      // the pieces of the queued tets, one per group, in full rounds (the
+      // rest of the queue at the end of the scan)
+      const int nround = scan_done ? nq : nq - nq % PIECE_NG;
+      for (int q0 = 0; q0 < nround && !abandon; q0 += PIECE_NG) {
+        const int qe = q0 + gid;
+        const bool has = qe < nround;
+        unsigned mk0 = has ? S.qmask[0][qe] : 0u, mk1 = has ? S.qmask[1][qe] : 0u;
+        const unsigned tb = PIECE_TET0 + 4 * gid;  // this group's tet face ids
+        if (has && gl < 4) {
+          const int4 q = tets[S.queue[qe]];
+          const float4 p = verts[gl == 0 ? q.x : gl == 1 ? q.y : gl == 2 ? q.z : q.w];
+          const float4 seed = S.seed;
+          S.corner[gid][gl] = make_float4(p.x - seed.x, p.y - seed.y, p.z - seed.z, 0.f);
+        }
+        __syncwarp();
+        WarpCell<PIECE_SL> c;
+        cell_clear(c);
+        float cw = 0.f;
+        if (has && gl < 4) {
+          // faces (c,b,d), (a,c,d), (b,a,d), (a,b,c) (voronoi.cu:179)
+          const int f0 = gl == 0 ? 2 : gl == 1 ? 0 : gl == 2 ? 1 : 0;
+          const int f1 = gl == 0 ? 1 : gl == 1 ? 2 : gl == 2 ? 0 : 1;
+          const int f2 = gl == 3 ? 2 : 3;
+          const float4 p0 = S.corner[gid][f0], p1 = S.corner[gid][f1], p2 = S.corner[gid][f2];
+          S.plane[tb + gl] = face_plane(make_float3(p0.x, p0.y, p0.z), make_float3(p1.x, p1.y, p1.z),
+                                        make_float3(p2.x, p2.y, p2.z));
+          // the corners as triangles of their three faces: a, d, c, b
+          const float4 p = S.corner[gid][gl == 0 ? 0 : gl == 1 ? 3 : gl == 2 ? 2 : 1];
+          c.tri[0] = gl == 0 ? pack_tri(tb + 1, tb + 3, tb + 2) : gl == 1 ? pack_tri(tb, tb + 1, tb + 2)
+                   : gl == 2 ? pack_tri(tb, tb + 3, tb + 1) : pack_tri(tb, tb + 2, tb + 3);
+          c.vx[0] = p.x;
+          c.vy[0] = p.y;
+          c.vz[0] = p.z;
+          c.vw[0] = norm2_rn(make_float3(p.x, p.y, p.z));
+          cw = c.vw[0];
+        }
+        c.vm[0] = has ? 0xfu : 0u;
+        c.nt = has ? 4 : 0;
+        c.r2 = group_max_nonneg<PIECE_G>(cw, gid);
+        __syncwarp();
+        // the crossing faces in turn; groups whose piece is done pass
+        int state = has ? 0 : 1;  // 0 piece, 1 empty, 2 dropped, 3 outgrew the group
+        bool act = has;
+        unsigned seq_cnt = 0u;  // planes (bits 0-7), cuts (8-15), vertex-vs-plane tests (16-31)
+        while (__any_sync(FULL, act && (mk0 | mk1) != 0u)) {
+          int f = -1;
+          if (act && mk0) {
+            f = __ffs(mk0) - 1;
+            mk0 &= mk0 - 1u;
+          } else if (act && mk1) {
+            f = 32 + __ffs(mk1) - 1;
+            mk1 &= mk1 - 1u;
+          }
+          const bool go = f >= 0;
+          const float4 P = S.plane[go ? f : 0];
+          if (go) seq_cnt += 1u + ((unsigned)c.nt << 16);
+          const int r = group_clip<PIECE_G, PIECE_SL, ROBUST>(c, P, (unsigned)(go ? f : 0), S.plane, S.conf[gid],
+                                                              S.bedge[gid], gl, gbase, gid, go, S.gnew + gid,
+                                                              S.cnt + WC_EXACT);
+          if (go) {
+            if (r == CLIP_CUT) seq_cnt += 1u << 8;
+            else if (r == CLIP_EMPTY) state = 1, act = false;
+            else if (r == CLIP_OVERFLOW) state = 3, act = false;
+            else if (r == CLIP_BOUNDARY) state = 2, act = false;
+          }
+        }
+        if (__any_sync(FULL, state == 3)) {
+          abandon = true;
+          break;
+        }
+        const bool piece = has && state == 0;
+        float vol = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+        if (__any_sync(FULL, piece)) group_moments<PIECE_G, PIECE_SL>(c, S.plane, gl, vol, mx, my, mz);
+        // into the site's sums, group by group (queue order)
+#pragma unroll
+        for (int g = 0; g < PIECE_NG; ++g) {
+          const int src = g * PIECE_G;
+          const int gstate = __shfl_sync(FULL, state, src);
+          const unsigned gseq = __shfl_sync(FULL, seq_cnt, src);
+          const float gv = __shfl_sync(FULL, vol, src), gx = __shfl_sync(FULL, mx, src);
+          const float gy = __shfl_sync(FULL, my, src), gz = __shfl_sync(FULL, mz, src);
+          const float gr2 = __shfl_sync(FULL, c.r2, src);
+          const int gnt = __shfl_sync(FULL, c.nt, src);
+          if (lane == 0 && q0 + g < nround) {
+            S.cnt[WC_PLANES] += gseq & 0xffu;
+            S.cnt[WC_CLIPS] += (gseq >> 8) & 0xffu;
+            S.cnt[WC_CONFLICT] += gseq >> 16;
+            if (gstate == 0) {
+              comp_add(S.acc[0], S.acc[4], gv);
+              comp_add(S.acc[1], S.acc[5], gx);
+              comp_add(S.acc[2], S.acc[6], gy);
+              comp_add(S.acc[3], S.acc[7], gz);
+              S.cnt[WC_CONTRIB]++;
+              S.cnt[WC_FINAL] += (unsigned)gnt;
+              // the largest |vertex - site|^2 of the site's pieces
+              if (S.site_flags & SITE_SECMISS) S.pr2 = fmaxf(S.pr2, gr2);
+            } else if (gstate == 1) {
+              S.cnt[WC_EMPTY]++;
+            } else {
+              S.cnt[WC_BOUNDARY]++;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      // the rest of the queue (less than a round) to its front
+      const int rem = nq - nround;
+      unsigned qt = 0u, qm0 = 0u, qm1 = 0u;
+      if (lane < rem) {
+        qt = S.queue[nround + lane];
+        qm0 = S.qmask[0][nround + lane];
+        qm1 = S.qmask[1][nround + lane];
+      }
+      __syncwarp();
+      if (lane < rem) {
+        S.queue[lane] = qt;
+        S.qmask[0][lane] = qm0;
+        S.qmask[1][lane] = qm1;
+      }
+      __syncwarp();
+      nq = rem;
+    }
+    if (abandon) {
+      // the 128-vertex pass redoes this site from scratch
+      if (lane == 0) {
+        out_list[atomicAdd(out_count, 1)] = s;
+        S.cnt[WC_REDO]++;
+        if (store.flags) store.flags[s] = (unsigned char)(S.site_flags | SITE_REDO);
+      }
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0) {
+      unsigned f = S.site_flags;
+      mom[s] = make_dmom4((double)S.acc[0] + (double)S.acc[4], (double)S.acc[1] + (double)S.acc[5],
+                          (double)S.acc[2] + (double)S.acc[6], (double)S.acc[3] + (double)S.acc[7]);
+      if (exact && esc_list && (f & SITE_SECMISS)) {
+        // as k_clip_site: exact when the pieces lie within half the K-th
+        // neighbour's distance, else completed by the completion pass
+        const int K = PD(K);
+        const float dK2 = dist2(S.seed, sites[knn[PD(knn_off) + (size_t)(s - PD(site_off)) * K + K - 1]]);
+        if (!(dK2 > __fmaf_rn(4.f * S.pr2, 1.0001f, 1e-4f))) {
+          const int pos = atomicAdd(esc_count, 1);
+          esc_list[pos] = s;
+          esc_r2[pos] = S.pr2;
+          f |= SITE_UNRESOLVED;
+        }
+      }
+      if (store.flags) store.flags[s] = (unsigned char)f;
+      if (f & SITE_SECMISS) {
+        S.cnt[WC_SECMISS]++;
+        if (prob_secmiss) atomicAdd(prob_secmiss + pidx, 1u);
+      }
+    }
+    __syncwarp();
+#undef PD
+  }
+  if (lane == 0)
+    for (int g = 0; g < PIECE_NG; ++g) S.cnt[WC_NEWV] += S.gnew[g];
+  __syncwarp();
   if (stats && lane < WC_N && S.cnt[lane]) atomicAdd(stats + stat_slot(lane), (unsigned long long)S.cnt[lane]);
 }
 
@@ -999,22 +1419,10 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_BUILD_MIN_BLOCKS) k_bui
     // bisector planes in site-relative coordinates: n = -b, w = |b|^2 / 2
     if (has) {
       const unsigned* krow = knn + PD(knn_off) + (size_t)(s - PD(site_off)) * K;
-      for (int j = gl; j < K1; j += G) {
-        const float4 B = sites[krow[j]];
-        const float bx = B.x - seed.x, by = B.y - seed.y, bz = B.z - seed.z;
-        const float bb = fmaf(bz, bz, fmaf(by, by, bx * bx));
-        plane[4 + j] = make_float4(-bx, -by, -bz, 0.5f * bb);
-      }
+      for (int j = gl; j < K1; j += G) plane[4 + j] = bisector_plane(seed, sites[krow[j]]);
     }
     // the start cube centred on the site, containing the domain box
-    constexpr float lo = -0.1f, hi = 1000.1f;
-    const float L = fmaxf(fmaxf(fmaxf(seed.x - lo, hi - seed.x), fmaxf(seed.y - lo, hi - seed.y)),
-                          fmaxf(seed.z - lo, hi - seed.z)) + 1.f;
-    if (gl < BOX_PLANES) {
-      const int ax = gl >> 1;
-      const float sgn = (gl & 1) ? -1.f : 1.f;
-      plane[4 + K + gl] = make_float4(ax == 0 ? sgn : 0.f, ax == 1 ? sgn : 0.f, ax == 2 ? sgn : 0.f, L);
-    }
+    if (gl < BOX_PLANES) plane[4 + K + gl] = start_plane(gl, seed, cube_half_side(seed));
     }
     __syncwarp();
     const float L = plane[4 + K].w;  // the start cube's half side
@@ -1192,9 +1600,9 @@ template <bool R>
 struct ClipPasses {
   // SMs x resident blocks per SM, per kernel variant: tet-cell, cell-tet lone
   // fast / redo, cell-tet batched fast / redo, completion lone / batched,
-  // the 96-vertex fast pass lone / batched
+  // the 96-vertex fast pass lone / batched, the pieces pass lone / batched
   static int* resident() {
-    static int r[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    static int r[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     return r;
   }
   static int prepare();
@@ -1223,7 +1631,8 @@ int ClipPasses<R>::prepare() {
       resident_blocks(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, sms, r + 5) ||
       resident_blocks(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, sms, r + 6) ||
       resident_blocks(k_clip_site<true, false, SLOTS_WIDE, R>, sms, r + 7) ||
-      resident_blocks(k_clip_site<true, true, SLOTS_WIDE, R>, sms, r + 8))
+      resident_blocks(k_clip_site<true, true, SLOTS_WIDE, R>, sms, r + 8) ||
+      resident_blocks(k_clip_pieces<false, R>, sms, r + 9) || resident_blocks(k_clip_pieces<true, R>, sms, r + 10))
     return -2;
   return 0;
 }
@@ -1281,23 +1690,28 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
     k_clip_site<false, false, SLOTS_TET_CELL, R><<<(int)(want < need ? want : need), CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, nullptr, nullptr,
         nullptr, nullptr, nullptr, nullptr, nullptr, prob_secmiss, nullptr, nullptr, nullptr, nullptr, nullptr,
-        CellStore{}, 0, nullptr, nullptr, nullptr, nullptr);
+        CellStore{}, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
     VGB_CUDA_TRY(cudaGetLastError());
     return 0;
   }
-  // counters: [0] sites the first pass hands on, [1] sites the one-warp pass
-  // hands on, [2..4] the three passes' work counters, [5] the kNN's, [8] deep
-  // sites (not done within the tier's neighbours), [9] their kNN's work
-  // counter, [10] sites to complete, [11] the completion pass's work
-  // counter; lists: [0, n) the one-warp pass's hand-offs, [n, 2n) the first
-  // pass's, [2n, 3n) the deep sites, [3n, 4n) the sites to complete and
-  // [4n, 5n) their pieces' squared radius bounds (float)
+  // counters: [0] sites the first pass hands on, [1] sites the one-warp and
+  // pieces passes hand to the 128-vertex pass, [2..4] the three passes' work
+  // counters, [5] the kNN's, [6] sites handed to the pieces pass, [7] its
+  // work counter, [8] deep sites (not done within the tier's neighbours),
+  // [9] their kNN's work counter, [10] sites to complete, [11] the
+  // completion pass's work counter; lists: [0, n) the hand-offs to the
+  // 128-vertex pass, [n, 2n) the first pass's, [2n, 3n) the deep sites,
+  // [3n, 4n) the sites to complete, [4n, 5n) their pieces' squared radius
+  // bounds (float) and [5n, 6n) the pieces pass's sites
   const bool exact = tet_order != nullptr;
   int* const redo = lists;
   int* const rest = lists + n;
   int* const deep = lists + 2 * (size_t)n;
   int* const esc = exact ? lists + 3 * (size_t)n : nullptr;
   float* const esc_r2 = exact ? reinterpret_cast<float*>(lists + 4 * (size_t)n) : nullptr;
+  // the pieces pass (cell-tet records needed)
+  const bool pieces = shape.pieces != 0 && store.faces != nullptr;
+  int* const piece_list = pieces ? lists + 5 * (size_t)n : nullptr;
   const int kt = exact ? k_tier : 0;
   VGB_CUDA_TRY(cudaMemsetAsync(counters, 0, 12 * sizeof(int), st));
   // every pass: one wave of resident blocks whose warps draw sites from a counter
@@ -1305,11 +1719,19 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
   CellStore cs = store;
   if (!exact) cs.tri = nullptr, cs.nt = nullptr;  // stored cells: exact form only
   auto launch = [&](auto kernel, int variant, const int* in_list, const int* in_count, int* out_list, int* out_count,
-                    int* work) {
+                    int* work, bool emit = false) {
     kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
         sites, n, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, field, field_sat,
         tet_order, tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, in_list, in_count, out_list,
-        out_count, work, cs, kt, cell_start, esc, esc_r2, exact ? counters + 10 : nullptr);
+        out_count, work, cs, kt, cell_start, esc, esc_r2, exact ? counters + 10 : nullptr,
+        emit ? piece_list : nullptr, emit ? counters + 6 : nullptr);
+  };
+  // the pieces pass over the sites the one-warp pass handed on
+  auto launch_pieces = [&](auto kernel, int variant) {
+    kernel<<<g_clip_resident_blocks[variant], CLIP_WARPS * WARP, 0, st>>>(
+        sites, knn, probs, site_prob, lone, verts, tets, site_start, site_tets, mom, stats, tet_order,
+        tet_cell_start, tet_sph, reach, reach_max_bits, prob_secmiss, piece_list, counters + 6, counters + 7,
+        redo, counters + 1, cs, esc, esc_r2, exact ? counters + 10 : nullptr);
   };
   if (exact) {
     if (kmax < 1 || kmax > MAX_SITE_K) {
@@ -1345,18 +1767,20 @@ int ClipPasses<R>::run(bool cell_tet, const float4* sites, int n, unsigned* knn,
   const bool wide = shape.fast_sl == SLOTS_WIDE;
   if (probs) {
     if (wide)
-      launch(k_clip_site<true, true, SLOTS_WIDE, R>, 8, in_list, in_count, redo, counters + 1, counters + 3);
+      launch(k_clip_site<true, true, SLOTS_WIDE, R>, 8, in_list, in_count, redo, counters + 1, counters + 3, pieces);
     else
-      launch(k_clip_site<true, true, SLOTS_FAST, R>, 3, in_list, in_count, redo, counters + 1, counters + 3);
+      launch(k_clip_site<true, true, SLOTS_FAST, R>, 3, in_list, in_count, redo, counters + 1, counters + 3, pieces);
+    if (pieces) launch_pieces(k_clip_pieces<true, R>, 10);
     launch(k_clip_site<true, true, SLOTS_REDO, R>, 4, redo, counters + 1, nullptr, nullptr, counters + 4);
     if (exact)
       launch(k_clip_site<true, true, SLOTS_COMPLETE, R, true>, 6, esc, counters + 10, nullptr, nullptr,
              counters + 11);
   } else {
     if (wide)
-      launch(k_clip_site<true, false, SLOTS_WIDE, R>, 7, in_list, in_count, redo, counters + 1, counters + 3);
+      launch(k_clip_site<true, false, SLOTS_WIDE, R>, 7, in_list, in_count, redo, counters + 1, counters + 3, pieces);
     else
-      launch(k_clip_site<true, false, SLOTS_FAST, R>, 1, in_list, in_count, redo, counters + 1, counters + 3);
+      launch(k_clip_site<true, false, SLOTS_FAST, R>, 1, in_list, in_count, redo, counters + 1, counters + 3, pieces);
+    if (pieces) launch_pieces(k_clip_pieces<false, R>, 9);
     launch(k_clip_site<true, false, SLOTS_REDO, R>, 2, redo, counters + 1, nullptr, nullptr, counters + 4);
     if (exact)
       launch(k_clip_site<true, false, SLOTS_COMPLETE, R, true>, 5, esc, counters + 10, nullptr, nullptr,

@@ -60,9 +60,9 @@ struct vgb_engine {
   float* reach = nullptr;          // exact form: per-tet reach (n_tet, centroid-cell order)
   float4* tet_sph = nullptr;       // exact form: tet bounding spheres (centroid-cell order)
   unsigned* reach_max = nullptr;   // exact form: float bits of the largest reach
-  int* redo_list = nullptr;        // cell-tet: sites handed from one clip pass to the next, deep sites (3n)
+  int* redo_list = nullptr;        // cell-tet: the clip passes' site lists (6n)
   int* redo_count = nullptr;       // clip hand-off and work counters, kNN work counters (12)
-  vgb::CellStore store{};          // exact form: cells the first clip pass built and handed on (by site)
+  vgb::CellStore store{};          // cells the first clip pass built and handed on, cell records (by site)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [update]
   cudaEvent_t ev[VGB_PHASES + 1] = {};
   cudaEvent_t tev[2] = {};
@@ -176,7 +176,7 @@ void free_engine(vgb_engine* e) {
   void* bufs[] = {e->verts, e->tets, e->sites, e->sites_tmp, e->cell_start, e->cell_fill, e->site_cell,
                   e->scan_tmp, e->pos_of_id, e->tet_order, e->tet_cell_start, e->knn, e->cand, e->site_start, e->site_fill, e->site_tets, e->mom, e->mom_f,
                   e->io_stage, e->stats, e->field, e->field_sat, e->reach, e->reach_max, e->tet_sph,
-                  e->redo_list, e->redo_count, e->store.tri, e->store.nt, e->store.flags};
+                  e->redo_list, e->redo_count, e->store.tri, e->store.nt, e->store.flags, e->store.faces};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (e->st) cudaStreamDestroy(e->st);
@@ -261,10 +261,12 @@ int tune_shapes(vgb_engine* e) {
   const bool was = e->timed;
   e->timed = false;
   KernelShape best{};
+  best.pieces = e->cfg.tet_pieces ? 1 : 0;
   float best_ms = 1e30f;
   int rc = VGB_OK;
   for (auto& sh : shapes) {
     KernelShape s{};
+    s.pieces = best.pieces;
     s.build_g = sh[0];
     s.fast_sl = sh[1];
     float ms = 0.f;
@@ -277,6 +279,7 @@ int tune_shapes(vgb_engine* e) {
     float ms = 0.f;
     if (!(rc = timed(s, &ms)) && ms < best_ms) best = s;
   }
+
   e->shape = best;
   e->timed = was;
   return rc;
@@ -324,6 +327,7 @@ void vgb_config_init(vgb_config* cfg) {
   cfg->exact = 0;
   cfg->robust_predicates = 0;
   cfg->autotune = 0;
+  cfg->tet_pieces = 0;
 }
 
 const char* vgb_last_error(void) { return vgb::last_error(); }
@@ -374,6 +378,7 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
   vgb_engine* e = new (std::nothrow) vgb_engine();
   if (!e) { set_error("host allocation failed"); return VGB_ERR_NOMEM; }
   e->cfg = cfg;
+  e->shape.pieces = cfg.tet_pieces ? 1 : 0;
   e->n_vert = n_vert; e->n_tet = n_tet; e->n = n_site;
   // site_k 0: autotuned after the upload; buffers sized for the largest K
   const int k_cap = std::min(MAX_SITE_K, n_site - 1);
@@ -407,12 +412,13 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
       (rc = dalloc(&e->knn, (size_t)n_site * e->K)) || (rc = dalloc(&e->cand, exact_form ? 1 : pairs)) ||
       (rc = dalloc(&e->site_start, (size_t)n_site + 1)) || (rc = dalloc(&e->site_fill, n_site)) ||
       (rc = dalloc(&e->site_tets, cfg.method != VGB_METHOD_PLAIN && !exact_form ? pairs : 1)) ||
-      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 5 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 12)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
+      (rc = dalloc(&e->mom, n_site)) || (rc = dalloc(&e->redo_list, 6 * (size_t)n_site)) || (rc = dalloc(&e->redo_count, 12)) || (rc = dalloc(&e->mom_f, cfg.method == VGB_METHOD_PLAIN ? n_site : 1)) ||
       (rc = dalloc(&e->io_stage, 3 * (size_t)std::max(n_site, n_vert))) ||
       (rc = dalloc(&e->stats, VGB_STAT_COUNT)) ||
       (rc = dalloc(&e->store.tri, exact_form ? (size_t)n_site * STORE_VERTS : 1)) ||
       (rc = dalloc(&e->store.nt, exact_form ? (size_t)n_site : 1)) ||
-      (rc = dalloc(&e->store.flags, cfg.method == VGB_METHOD_CELL_TET ? (size_t)n_site : 1))) {
+      (rc = dalloc(&e->store.flags, cfg.method == VGB_METHOD_CELL_TET ? (size_t)n_site : 1)) ||
+      (rc = dalloc(&e->store.faces, cfg.method == VGB_METHOD_CELL_TET ? (size_t)n_site * PIECE_REC : 1))) {
     free_engine(e);
     return rc;
   }
@@ -677,11 +683,12 @@ void vgb_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
 
-int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots) {
+int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots, int* tet_pieces) {
   if (!e) { set_error("NULL engine"); return VGB_ERR_INVALID; }
   if (knn_warps) *knn_warps = e->shape.knn_warps;
   if (build_lanes) *build_lanes = e->shape.build_g;
   if (fast_slots) *fast_slots = e->shape.fast_sl;
+  if (tet_pieces) *tet_pieces = e->shape.pieces;
   return VGB_OK;
 }
 

@@ -151,6 +151,10 @@ struct KernelShape {
   int knn_warps = 8;
   int build_g = 8;
   int fast_sl = 2;
+  // cell-tet method: 1 builds each piece (cell ^ tet) from its tet, clipped
+  // by the cell faces that cross it, four per warp (the pieces pass); 0 clips
+  // a copy of the cell by each tet inside the one-warp pass
+  int pieces = 0;
 };
 
 // Exclusive scan of n ints (in may alias out).  tmp must hold scan_tmp_ints(n).
@@ -248,7 +252,13 @@ struct CellStore {
   unsigned* tri;         // [n][STORE_VERTS]
   int* nt;               // [n]
   unsigned char* flags;  // [n] SITE_* bits of the last pass (cell-tet method), may be null
+  unsigned* faces;       // [n][PIECE_REC] cell records for the pieces pass (cell-tet method), may be null
 };
+// A cell record of the one-warp pass for the pieces pass: its face count,
+// radius (float bits) and outcome bits so far, a spare word, then its face
+// plane ids (8 bits each, at most PIECE_FACES).
+constexpr int PIECE_FACES = 64;
+constexpr int PIECE_REC = 4 + PIECE_FACES / 4;
 
 int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, const ProbDesc* probs,
                     const int* site_prob, const ProbDesc& lone, const float4* verts, const int4* tets,
@@ -269,9 +279,9 @@ int clip_site_major(bool cell_tet, const float4* sites, int n, unsigned* knn, co
 // form): the neighbour rows hold only their first min(K, k_tier) entries (the
 // kNN ran with that tier); the first pass builds from them, and the rows of
 // the sites it leaves unfinished are completed (knn_sites_listed, from
-// cell_start and pos_of_id) before the one-warp pass.  lists: 5n ints,
-// counters: at least 12 (the exact form's completion list and its counters
-// among them).
+// cell_start and pos_of_id) before the one-warp pass.  lists: 6n ints,
+// counters: at least 12 (the exact form's completion list, the pieces pass's
+// list and their counters among them).
 
 // Inside field of one problem: turn the inside flags (fdim^3 bytes) into
 // 1 + the clear radius in cells, from the summed table of touched cells.

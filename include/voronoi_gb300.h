@@ -137,6 +137,14 @@ typedef struct vgb_config {
                    cell in the one-warp clip pass (64 or 96); results do not depend on
                    them beyond float rounding.  0: the defaults (8, 8, 64).  The
                    batched form tunes them with the grid density (grid_dim 0).       */
+  int tet_pieces; /* cell-tet method.  0 (default): a copy of the cell is clipped by
+                   each candidate tet's four faces, one warp per site.  1: each piece
+                   (cell ^ tet) of a cell the first pass does not finish is built
+                   from its tet, clipped by the cell faces that cross the tet, four
+                   tets per warp (the pieces pass).  The same pieces up to float
+                   rounding; on relaxed uniform sites the first is about 10% faster
+                   (the pieces have a quarter of the cell's vertices, but each needs
+                   about eight cuts to the copy's four).                            */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;
@@ -211,8 +219,10 @@ int vgb_engine_info(vgb_engine* e, int* n_site, int* n_tet, int* site_k, int* te
 
 /* Launch shapes in use (autotuned with cfg.autotune): warps per kNN block,
  * lanes per site in the first clip pass, triangle slots per lane of the
- * one-warp clip pass (32 x slots vertices).  Any pointer may be NULL. */
-int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots);
+ * one-warp clip pass (32 x slots vertices), and the clip form (1: pieces
+ * built from their tets, 0: copies of the cell clipped by each tet; see
+ * vgb_config.tet_pieces).  Any pointer may be NULL. */
+int vgb_engine_shape(vgb_engine* e, int* knn_warps, int* build_lanes, int* fast_slots, int* tet_pieces);
 
 /* Device time in ms of the phases of the last non-graph pass:
  * [0] grid sort, [1] site kNN, [2] tet candidates, [3] site-major candidate
@@ -277,7 +287,7 @@ int vgb_batch_sync(vgb_batch* b);
 int vgb_batch_time_iterate(vgb_batch* b, int n_iter, int update, float* ms);
 int vgb_batch_info(const vgb_batch* b, int* n_prob, int* n_site_total, int* n_tet_total, float* density);
 /* Launch shapes the batch's autotuner kept (as vgb_engine_shape). */
-int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots);
+int vgb_batch_shape(const vgb_batch* b, int* knn_warps, int* build_lanes, int* fast_slots, int* tet_pieces);
 /* Sizes and the tuned parameters of problem p. */
 int vgb_batch_problem(const vgb_batch* b, int p, int* n_site, int* n_tet, int* site_k, int* grid_dim,
                       int* field_dim);

@@ -134,8 +134,9 @@ def test_autotuned_shapes_give_the_same_cells(pkg, meshgen, oracle):
             vol[ids] = vol_g
             runs.append((shape, vol))
     (s0, v0), (s1, v1) = runs
-    assert s0 == {"knn_warps": 8, "build_lanes": 8, "fast_vertices": 64}
+    assert s0 == {"knn_warps": 8, "build_lanes": 8, "fast_vertices": 64, "tet_pieces": 0}
     assert s1["knn_warps"] in (4, 8) and s1["build_lanes"] in (8, 16) and s1["fast_vertices"] in (64, 96)
+    assert s1["tet_pieces"] in (0, 1)
     big = v0 > 1e-9 * v0.max()
     assert (np.abs(v1[big] - v0[big]) / v0[big]).max() < 1e-5
     mv = oracle.mesh_volume(P.verts, P.tets)
@@ -144,3 +145,4 @@ def test_autotuned_shapes_give_the_same_cells(pkg, meshgen, oracle):
     with pkg.Batch([(Q.verts, Q.tets, Q.sites) for Q in probs], site_k=0, tune_grid=True) as B:
         bs = B.shape()
     assert bs["knn_warps"] in (4, 8) and bs["build_lanes"] in (8, 16) and bs["fast_vertices"] in (64, 96)
+    assert bs["tet_pieces"] in (0, 1)

@@ -269,17 +269,19 @@ def test_invalid_arguments_raise(built, meshgen):
         pkg.Engine(P.verts, P.tets, P.sites, site_k=200)  # above the supported maximum
 
 
-def test_exact_form_matches_oracle(built, meshgen, oracle):
+@pytest.mark.parametrize("tet_pieces", [True, False])
+def test_exact_form_matches_oracle(built, meshgen, oracle, tet_pieces):
     """Exact form: cells that provably lie inside the mesh are taken whole,
-    the others are clipped by every tet within reach, and a cell whose K
-    neighbours leave it unresolved (the cube's corner cells at K = 64) is
-    completed: every cell is the exact clipped cell, so the bar is the
-    oracle's exact cells (complete neighbour lists), and the volume is
+    the others are clipped by every tet within reach (as pieces built from
+    their tets, or as copies of the cell clipped by each tet), and a cell
+    whose K neighbours leave it unresolved (the cube's corner cells at
+    K = 64) is completed: every cell is the exact clipped cell, so the bar is
+    the oracle's exact cells (complete neighbour lists), and the volume is
     conserved.  (The reference with K = 64 overshoots the mesh volume by
     1-2e-5 here: its corner cells miss clipping neighbours.)"""
     pkg = built
     P = meshgen.cube_problem(20, 20000, seed=1)
-    g = run_engine_by_id(pkg, P, site_k=64, exact=True)
+    g = run_engine_by_id(pkg, P, site_k=64, exact=True, tet_pieces=tet_pieces)
     # the exact form sizes its grid by the sites' density in the mesh, so
     # its grid order may differ from the oracle's: compare by site id
     assert g["stats"]["interior"] > len(P.sites) // 5
@@ -287,14 +289,32 @@ def test_exact_form_matches_oracle(built, meshgen, oracle):
     check_exact_cells(oracle, P, g["vol"], g["mom"], g["flags"], secmiss_bit=pkg.SITE_SECMISS)
 
 
-def test_exact_form_on_torus(built, meshgen, oracle):
+@pytest.mark.parametrize("tet_pieces", [True, False])
+def test_exact_form_on_torus(built, meshgen, oracle, tet_pieces):
     """A non-convex mesh: the voxelised torus (32^3), uniform sites; every
-    cell against the oracle's exact cells."""
+    cell against the oracle's exact cells, with either clip form."""
     pkg = built
     P = meshgen.torus_problem(6000, grid=32, seed=4)
-    g = run_engine_by_id(pkg, P, site_k=64, exact=True)
+    g = run_engine_by_id(pkg, P, site_k=64, exact=True, tet_pieces=tet_pieces)
     assert g["stats"]["interior"] > 0 and g["stats"]["unresolved"] == 0
     check_exact_cells(oracle, P, g["vol"], g["mom"], g["flags"], n_sample=6000, secmiss_bit=pkg.SITE_SECMISS)
+
+
+def test_pieces_outgrowing_their_group_are_redone(built, meshgen, oracle):
+    """Tets much larger than the cells (a cube of six Kuhn tets, 3,000
+    sites): a piece is most of a boundary cell, and the pieces that outgrow
+    a lane group's 32 vertices send their site to the 128-vertex pass, which
+    redoes it with copies of the cell.  Every cell against the oracle's exact
+    cells."""
+    pkg = built
+    P = meshgen.cube_problem(1, 3000, seed=8)
+    # (tet_k only sizes the reference form's candidate sets; its default
+    # for 3,000 sites over 6 tets is above the supported 128)
+    g = run_engine_by_id(pkg, P, site_k=64, tet_k=6, exact=True, tet_pieces=True)
+    st = g["stats"]
+    assert st["redo"] >= 1 and st["unresolved"] == 0
+    assert st["tri_overflow"] == 0 and st["boundary_fail"] == 0
+    check_exact_cells(oracle, P, g["vol"], g["mom"], g["flags"], n_sample=3000, secmiss_bit=pkg.SITE_SECMISS)
 
 
 def test_large_cells_redone(built, meshgen, oracle):
