@@ -1256,8 +1256,8 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_PIECE_MIN_BLOCKS) k_cli
           const float4 P = S.plane[go ? f : 0];
           if (go) seq_cnt += 1u + ((unsigned)c.nt << 16);
           const int r = group_clip<PIECE_G, PIECE_SL, ROBUST>(c, P, (unsigned)(go ? f : 0), S.plane, S.conf[gid],
-                                                              S.bedge[gid], gl, gbase, gid, go, S.gnew + gid,
-                                                              S.cnt + WC_EXACT);
+                                                              S.bedge[gid], PIECE_G * PIECE_SL, gl, gbase, gid, go,
+                                                              S.gnew + gid, S.cnt + WC_EXACT);
           if (go) {
             if (r == CLIP_CUT) seq_cnt += 1u << 8;
             else if (r == CLIP_EMPTY) state = 1, act = false;
@@ -1449,7 +1449,9 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_BUILD_MIN_BLOCKS) k_bui
     while (__any_sync(FULL, building)) {
       const float4 P = building ? plane[pi] : make_float4(0.f, 0.f, 0.f, 1.f);
       if (building) seq_cnt += 1u + ((unsigned)c.nt << 16);
-      const int r = group_clip<G, SL, ROBUST>(c, P, (unsigned)pi, plane, S.conf, S.bedge, gl, gbase, gid, building,
+      const int r = group_clip<G, SL, ROBUST>(c, P, (unsigned)pi, plane, S.conf, S.bedge,
+                                              (int)(sizeof(BuildSmem<G * SL>) / sizeof(unsigned)), gl, gbase, gid,
+                                              building,
                                               S.cnt + WC_NEWV, S.cnt + WC_EXACT);
       if (building) {
         if (r == CLIP_EMPTY) {

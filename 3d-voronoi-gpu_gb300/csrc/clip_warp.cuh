@@ -470,31 +470,48 @@ __device__ __forceinline__ unsigned group_min_u(unsigned v, int gid) {
 // warp_clip for the cell of a lane group (act: this group clips; the others
 // only take part in the collectives).  The same steps: remove the vertices
 // strictly outside P; a directed edge of a removed triangle is on the
-// cavity boundary when no removed triangle holds its twin (each edge lane
-// searches the group's removed triangles); each boundary vertex must start
-// and end exactly one boundary edge; the fan (pidx, a, b) fills freed slots.
-// Returns the group's result; the cell is changed only on CLIP_CUT.  conf and
-// bedge: the group's G SL-entry scratch arrays; nnew (the group's, shared,
-// may be null): the group's lane 0 adds the vertices a cut creates.
+// cavity boundary when no removed triangle holds its twin; each boundary
+// vertex must start and end exactly one boundary edge; the fan (pidx, a, b)
+// fills freed slots.  When the cutting groups' edges fit in the warp (three
+// per removed triangle, summed over the groups, at most 32), one edge per
+// lane, a __match_any_sync on keys made unique per group -- (group, a, b)
+// with a < b -- finds every twin at once, and a second one on (group, a)
+// finds boundary vertices that start two edges; otherwise each group
+// searches its removed triangles G edges at a time.  Loops over slots stop
+// at the highest slot any group uses.  Returns the group's result; the cell
+// is changed only on CLIP_CUT.  conf and bedge: the group's G SL-entry
+// scratch arrays, gstride words after the previous group's; nnew (the
+// group's, shared, may be null): the group's lane 0 adds the vertices a cut
+// creates.
 template <int G, int SL, bool ROBUST = false>
 __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const unsigned pidx, const float4* planes,
-                                          unsigned* conf, unsigned* bedge, const int gl, const int gbase,
-                                          const int gid, const bool act, unsigned* nnew = nullptr,
+                                          unsigned* conf, unsigned* bedge, const int gstride, const int gl,
+                                          const int gbase, const int gid, const bool act, unsigned* nnew = nullptr,
                                           unsigned* nexact = nullptr) {
-  constexpr int CAP = G * SL;
+  constexpr int CAP = G * SL, NG = WARP / G;
+  const int lane = gbase + gl;
   const unsigned lb = 1u << gl, ltm = lb - 1u;
+  // slots that may hold a live vertex, over every group of the warp
+  int hs = 0;
+#pragma unroll
+  for (int k = 0; k < SL; ++k)
+    if (c.vm[k]) hs = k + 1;
+  const int kmax = SL == 1 ? 1 : (int)__reduce_max_sync(FULL, (unsigned)hs);
   unsigned m[SL];
   int nconf = 0;
   float lm = 0.f;  // largest |v|^2 of the vertices kept
 #pragma unroll
   for (int k = 0; k < SL; ++k) {
-    const bool live = c.vm[k] & lb;
-    const bool cf = act && live &&
-                    (ROBUST ? vertex_outside_robust(P, c.vx[k], c.vy[k], c.vz[k], c.tri[k], planes, nexact)
-                            : plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f);
-    m[k] = group_ballot<G>(cf, gbase);
-    nconf += __popc(m[k]);
-    if (live && !cf) lm = fmaxf(lm, c.vw[k]);
+    m[k] = 0u;
+    if (k < kmax) {
+      const bool live = c.vm[k] & lb;
+      const bool cf = act && live &&
+                      (ROBUST ? vertex_outside_robust(P, c.vx[k], c.vy[k], c.vz[k], c.tri[k], planes, nexact)
+                              : plane_eval(P, c.vx[k], c.vy[k], c.vz[k]) < 0.f);
+      m[k] = group_ballot<G>(cf, gbase);
+      nconf += __popc(m[k]);
+      if (live && !cf) lm = fmaxf(lm, c.vw[k]);
+    }
   }
   const bool cut = act && nconf > 0 && nconf < c.nt;
   int res = (!act || nconf == 0) ? CLIP_NONE : nconf == c.nt ? CLIP_EMPTY : CLIP_CUT;
@@ -504,57 +521,95 @@ __device__ __forceinline__ int group_clip(WarpCell<SL>& c, const float4 P, const
     int off = 0;
 #pragma unroll
     for (int k = 0; k < SL; ++k) {
-      if (cut && (m[k] & lb)) conf[off + __popc(m[k] & ltm)] = c.tri[k];
-      off += __popc(m[k]);
+      if (k < kmax) {
+        if (cut && (m[k] & lb)) conf[off + __popc(m[k] & ltm)] = c.tri[k];
+        off += __popc(m[k]);
+      }
     }
   }
   __syncwarp();
-  // boundary edges, G at a time
   const int E = 3 * R;
-  const int Emax = (int)__reduce_max_sync(FULL, (unsigned)E);
+  // the groups' edge counts as one run over the warp: this group's offset,
+  // and the group (gi) and offset (go) of the run's edge at this lane
+  int etot = 0, my_off = 0, gi = 0, go = 0;
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    const int Eg = NG == 1 ? E : __shfl_sync(FULL, E, g * G);
+    if (Eg > 0 && lane >= etot) gi = g, go = etot;
+    if (g < gid) my_off += Eg;
+    etot += Eg;
+  }
   int nb = 0;
-  for (int e0 = 0; e0 < Emax; e0 += G) {
-    const int e = e0 + gl;
-    bool isb = false;
-    unsigned ea = 0, eb = 0;
-    if (e < E) {
-      const unsigned T = conf[e / 3];
+  bool bad = false;
+  if (etot <= WARP) {
+    const bool has_e = lane < etot;
+    unsigned ea = 0u, eb = 0u, key = 0x80000000u | (unsigned)lane;
+    if (has_e) {
+      const int e = lane - go;
+      const unsigned T = conf[(gi - gid) * gstride + e / 3];
       const int es = e % 3;
       ea = tri_at(T, es);
       eb = tri_at(T, es == 2 ? 0 : es + 1);
-      // the twin (eb -> ea) as a directed-edge code lo | hi << 8; the codes
-      // of U = (u0, u1, u2) are its bytes 0-1, 1-2 and 2-0
-      const unsigned tw = eb | (ea << 8);
-      bool twin = false;
-      for (int q = 0; q < R; ++q) {
-        const unsigned U = conf[q];
-        twin |= ((U & 0xffffu) == tw) | (((U >> 8) & 0xffffu) == tw) | (__byte_perm(U, 0u, 0x4402u) == tw);
+      key = ((unsigned)gi << 16) | min(ea, eb) | (max(ea, eb) << 8);
+    }
+    // (every lane takes part in both matches, whatever its edge)
+    const unsigned same = __match_any_sync(FULL, key);
+    const bool isb = has_e && __popc(same) == 1;
+    const unsigned bm = __ballot_sync(FULL, isb);
+    if (isb) bedge[(gi - gid) * gstride + __popc(bm & ((1u << lane) - 1u) & ~((1u << go) - 1u))] = ea | (eb << 8);
+    const unsigned gmask = E == 0 ? 0u : ((1u << E) - 1u) << my_off;
+    nb = __popc(bm & gmask);
+    // each boundary vertex starts exactly one edge
+    const unsigned skey = isb ? (((unsigned)gi << 16) | ea) : (0x80000000u | (unsigned)lane);
+    const unsigned starts = __match_any_sync(FULL, skey);
+    const bool dup = isb && __popc(starts) != 1;
+    bad = (__ballot_sync(FULL, dup) & gmask) != 0u;
+  } else {
+    // boundary edges, G at a time
+    const int Emax = (int)__reduce_max_sync(FULL, (unsigned)E);
+    for (int e0 = 0; e0 < Emax; e0 += G) {
+      const int e = e0 + gl;
+      bool isb = false;
+      unsigned ea = 0, eb = 0;
+      if (e < E) {
+        const unsigned T = conf[e / 3];
+        const int es = e % 3;
+        ea = tri_at(T, es);
+        eb = tri_at(T, es == 2 ? 0 : es + 1);
+        // the twin (eb -> ea) as a directed-edge code lo | hi << 8; the codes
+        // of U = (u0, u1, u2) are its bytes 0-1, 1-2 and 2-0
+        const unsigned tw = eb | (ea << 8);
+        bool twin = false;
+        for (int q = 0; q < R; ++q) {
+          const unsigned U = conf[q];
+          twin |= ((U & 0xffffu) == tw) | (((U >> 8) & 0xffffu) == tw) | (__byte_perm(U, 0u, 0x4402u) == tw);
+        }
+        isb = !twin;
       }
-      isb = !twin;
+      const unsigned bm = group_ballot<G>(isb, gbase);
+      if (isb) {
+        const int r = nb + __popc(bm & ltm);
+        if (r < CAP) bedge[r] = ea | (eb << 8);
+      }
+      nb += __popc(bm);
     }
-    const unsigned bm = group_ballot<G>(isb, gbase);
-    if (isb) {
-      const int r = nb + __popc(bm & ltm);
-      if (r < CAP) bedge[r] = ea | (eb << 8);
+    __syncwarp();
+    // a cavity of more than three triangles edge by edge: each boundary
+    // vertex starts exactly one edge
+    const int nbc = (cut && R > 3 && nb <= CAP) ? nb : 0;
+    const int NBmax = (int)__reduce_max_sync(FULL, (unsigned)nbc);
+    for (int e0 = 0; e0 < NBmax; e0 += G) {
+      const int e = e0 + gl;
+      if (e < nbc) {
+        const unsigned Ed = bedge[e];
+        int starts = 0;
+        for (int q = 0; q < nbc; ++q) starts += (bedge[q] & 0xffu) == (Ed & 0xffu);
+        bad |= starts != 1;
+      }
     }
-    nb += __popc(bm);
+    bad = group_ballot<G>(bad, gbase) != 0u;
   }
-  __syncwarp();
-  // a cavity of at most three triangles by its edge count; a larger one
-  // edge by edge: each boundary vertex starts exactly one edge
-  const int nbc = (cut && R > 3 && nb <= CAP) ? nb : 0;
-  const int NBmax = (int)__reduce_max_sync(FULL, (unsigned)nbc);
-  bool bad = false;
-  for (int e0 = 0; e0 < NBmax; e0 += G) {
-    const int e = e0 + gl;
-    if (e < nbc) {
-      const unsigned Ed = bedge[e];
-      int starts = 0;
-      for (int q = 0; q < nbc; ++q) starts += (bedge[q] & 0xffu) == (Ed & 0xffu);
-      bad |= starts != 1;
-    }
-  }
-  bad = group_ballot<G>(bad, gbase) != 0u;
+  // a cavity of at most three triangles by its edge count
   if (cut && R <= 3) bad = !cavity_disk_small(R, nb);
   const int nt2 = c.nt - R + nb;
   if (cut) {
