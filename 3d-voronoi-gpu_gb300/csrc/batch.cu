@@ -18,9 +18,10 @@
 //
 // The autotuner (at creation) picks per problem the smallest K in
 // {32, 48, 64, 96, 128} whose cells all reach the security radius -- more
-// neighbours cannot change such a cell, so the result is the one of any
-// larger K -- and for the batch the grid density (sites per cell) with the
-// fastest measured pass.
+// neighbours cannot change such a cell -- then caps every K at the smaller
+// candidate with the fastest measured pass that leaves no cell unresolved
+// (the completion pass keeps the cells exact below that rule), and for the
+// batch the grid density (sites per cell) with the fastest measured pass.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -362,9 +363,11 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     free_batch(b);
     return VGB_ERR_CUDA;
   }
-  // concatenated inputs
+  // concatenated inputs (the sites kept on the host until the autotuner,
+  // which times relaxed sites, has put them back)
+  std::vector<float4> hs((size_t)b->n);
   {
-    std::vector<float4> hv((size_t)b->n_vert), hs((size_t)b->n);
+    std::vector<float4> hv((size_t)b->n_vert);
     std::vector<int4> ht((size_t)b->n_tet);
     std::vector<int> sp((size_t)b->n), tp((size_t)b->n_tet);
     std::vector<unsigned char> fld((size_t)f_off);
@@ -410,8 +413,24 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
       }
   }
   if ((rc = layout(b))) { free_batch(b); return rc; }
+// two passes timed after one untimed, on the current layout
+  auto timed = [&](float* ms) {
+    int r0 = batch_pass(b, 0, false);
+    if (r0) return r0;
+    cudaError_t te = cudaEventRecord(b->tev[0], b->st);
+    for (int r = 0; r < 2 && te == cudaSuccess && r0 == VGB_OK; ++r) r0 = batch_pass(b, 0, false);
+    if (te == cudaSuccess) te = cudaEventRecord(b->tev[1], b->st);
+    if (te == cudaSuccess) te = cudaEventSynchronize(b->tev[1]);
+    if (te == cudaSuccess) te = cudaEventElapsedTime(ms, b->tev[0], b->tev[1]);
+    if (!r0 && te != cudaSuccess) {
+      set_error("autotune timing: %s", cudaGetErrorString(te));
+      r0 = VGB_ERR_CUDA;
+    }
+    return r0;
+  };
   if (cfg.site_k == 0) {
-    // K: the smallest candidate whose cells all reach the security radius
+    // K per problem: the smallest candidate whose cells all reach the
+    // security radius
     static const int cand[] = {32, 48, 64, 96, MAX_SITE_K};
     std::vector<char> done(n_prob, 0);
     std::vector<unsigned> miss(n_prob);
@@ -431,22 +450,41 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
         if (!done[p] && (miss[p] == 0 || b->probs[p].K == b->site_cap[p])) done[p] = 1;
     }
   }
+  // the timed choices below are made on sites after two Lloyd steps, which
+  // behave like the rest of a run (the initial sites, random here, make
+  // larger cells and more boundary work); the initial sites are put back
+  // after them
+  const bool tune = cfg.site_k == 0 || cfg.grid_dim == 0;
+  if (tune)
+    for (int r = 0; r < 2; ++r)
+      if ((rc = batch_pass(b, 1, false))) { free_batch(b); return rc; }
+  if (cfg.site_k == 0) {
+    static const int cand[] = {32, 48, 64, 96, MAX_SITE_K};
+    // the rule's K capped at a smaller candidate, when that is faster and
+    // leaves no cell unresolved: the completion pass makes the cells exact
+    // whatever K, so a cap only moves work from the neighbour rows to its
+    // site-grid search
+    std::vector<int> rule(n_prob);
+    int kbig = 0;
+    for (int p = 0; p < n_prob; ++p) kbig = std::max(kbig, rule[p] = b->probs[p].K);
+    float best_ms = 0.f;
+    int best_cap = kbig;
+    if ((rc = layout(b)) || (rc = timed(&best_ms))) { free_batch(b); return rc; }
+    for (int ci = 0; ci < 4 && cand[ci] < kbig; ++ci) {
+      for (int p = 0; p < n_prob; ++p) b->probs[p].K = std::min(rule[p], cand[ci]);
+      unsigned long long st[VGB_STAT_COUNT];
+      if ((rc = layout(b)) || (rc = batch_pass(b, 0, false))) { free_batch(b); return rc; }
+      ce = cudaMemcpyAsync(st, b->stats, sizeof(st), cudaMemcpyDeviceToHost, b->st);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->st);
+      if (ce != cudaSuccess) { set_error("autotune: %s", cudaGetErrorString(ce)); free_batch(b); return VGB_ERR_CUDA; }
+      if (st[VGB_STAT_UNRESOLVED] != 0) continue;
+      float ms = 0.f;
+      if ((rc = timed(&ms))) { free_batch(b); return rc; }
+      if (ms < best_ms) best_ms = ms, best_cap = cand[ci];
+    }
+    for (int p = 0; p < n_prob; ++p) b->probs[p].K = std::min(rule[p], best_cap);
+  }
   if (cfg.grid_dim == 0) {
-    // two passes timed after one untimed, on the current layout
-    auto timed = [&](float* ms) {
-      int r0 = batch_pass(b, 0, false);
-      if (r0) return r0;
-      cudaError_t te = cudaEventRecord(b->tev[0], b->st);
-      for (int r = 0; r < 2 && te == cudaSuccess && r0 == VGB_OK; ++r) r0 = batch_pass(b, 0, false);
-      if (te == cudaSuccess) te = cudaEventRecord(b->tev[1], b->st);
-      if (te == cudaSuccess) te = cudaEventSynchronize(b->tev[1]);
-      if (te == cudaSuccess) te = cudaEventElapsedTime(ms, b->tev[0], b->tev[1]);
-      if (!r0 && te != cudaSuccess) {
-        set_error("autotune timing: %s", cudaGetErrorString(te));
-        r0 = VGB_ERR_CUDA;
-      }
-      return r0;
-    };
     // grid density: the fastest of three
     static const float dens[] = {1.5f, 3.1f, 6.0f};
     float best_ms = 1e30f, best = 3.1f;
@@ -460,7 +498,7 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     if ((rc = layout(b))) { free_batch(b); return rc; }
     // launch shapes: the four clip shapes (first-pass lane groups of 8 or
     // 16, one-warp pass of 64 or 96 vertices) with 8-warp kNN blocks, then
-    // the fastest with 4-warp kNN blocks
+    // the fastest with 4-warp kNN blocks, then with the other clip form
     static const int shapes[4][2] = {{8, 2}, {16, 2}, {8, 3}, {16, 3}};
     vgb::KernelShape bs{};
     bs.pieces = b->cfg.tet_pieces ? 1 : 0;
@@ -480,9 +518,18 @@ int vgb_batch_create(vgb_batch** out, const vgb_config* cfg_in, int n_prob, cons
     b->shape = t;
     float ms = 0.f;
     if ((rc = timed(&ms))) { free_batch(b); return rc; }
+    if (ms < bms) bs = t, bms = ms;
+    t = bs;
+    t.pieces = 1 - bs.pieces;
+    b->shape = t;
+    if ((rc = timed(&ms))) { free_batch(b); return rc; }
     b->shape = ms < bms ? t : bs;
   }
   if ((rc = layout(b))) { free_batch(b); return rc; }
+  if (tune) {
+    // the initial sites back (in input order: the passes sorted them)
+    VGB_CUDA_TRY(cudaMemcpy(b->sites, hs.data(), sizeof(float4) * hs.size(), cudaMemcpyHostToDevice));
+  }
   *out = b;
   return VGB_OK;
 }

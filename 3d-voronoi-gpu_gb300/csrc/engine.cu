@@ -243,7 +243,8 @@ int run_pass(vgb_engine* e, int update) {
 // Autotuner of the launch shapes: each candidate timed over two passes (after
 // one untimed) on the current sites with CUDA events -- the four clip shapes
 // (first-pass lane groups of 8 or 16, one-warp pass of 64 or 96 vertices)
-// with 8-warp kNN blocks, then the fastest of them with 4-warp kNN blocks.
+// with 8-warp kNN blocks, then the fastest of them with 4-warp kNN blocks,
+// then with the other clip form (copies of the cell or pieces from the tets).
 int tune_shapes(vgb_engine* e) {
   static const int shapes[4][2] = {{8, 2}, {16, 2}, {8, 3}, {16, 3}};
   auto timed = [&](const KernelShape& s, float* ms) {
@@ -277,9 +278,15 @@ int tune_shapes(vgb_engine* e) {
     KernelShape s = best;
     s.knn_warps = 4;
     float ms = 0.f;
+    if (!(rc = timed(s, &ms)) && ms < best_ms) best = s, best_ms = ms;
+  }
+  if (!rc) {
+    // the other clip form
+    KernelShape s = best;
+    s.pieces = 1 - best.pieces;
+    float ms = 0.f;
     if (!(rc = timed(s, &ms)) && ms < best_ms) best = s;
   }
-
   e->shape = best;
   e->timed = was;
   return rc;
@@ -506,21 +513,65 @@ int vgb_engine_create(vgb_engine** out, const vgb_config* cfg_in, const float* v
     if (field_clear_radius(e->field, e->field_sat, e->fdim, e->st)) { free_engine(e); return VGB_ERR_CUDA; }
   }
   if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
+  // The exact form's timed choices (K, launch shapes, clip form) are made on
+  // the sites after two Lloyd steps, which behave like the rest of a run
+  // (initial sites, random ones especially, make larger cells and more
+  // boundary work); the initial sites are put back after them.
+  const bool tune_exact = exact_form && (cfg.site_k == 0 || cfg.autotune);
+  if (tune_exact) {
+    if (cfg.site_k == 0) e->K = e->prob.K = std::min(64, k_cap);
+    for (int r = 0; r < 2; ++r)
+      if ((rc = run_pass(e, 1))) { free_engine(e); return rc; }
+  }
   if (cfg.site_k == 0) {
-    // K: the smallest of 32, 48, 64, 96, 128 (at most n - 1) whose cells all
-    // reach the security radius -- more neighbours cannot change such a cell
     static const int cand[] = {32, 48, 64, 96, MAX_SITE_K};
-    for (int k : cand) {
-      e->K = e->prob.K = std::min(k, k_cap);
-      unsigned long long st[VGB_STAT_COUNT];
-      if ((rc = run_pass(e, 0)) || (rc = vgb_engine_get_stats(e, st))) { free_engine(e); return rc; }
-      if (st[VGB_STAT_SECURITY_MISS] == 0 || e->K == k_cap) break;
+    if (exact_form) {
+      // K: the fastest of 32, 48, 64, 96, 128 (at most n - 1) whose pass
+      // leaves no cell unresolved.  The completion pass
+      // makes every cell exact whatever K, so K only moves work between the
+      // kNN rows and the completion's site-grid search; a K whose completion
+      // gave up on a cell is not taken.  Each candidate: one pass for its
+      // counters, two timed with CUDA events.
+      const bool was = e->timed;
+      e->timed = false;
+      int best = -1;
+      float best_ms = 0.f;
+      for (int k : cand) {
+        e->K = e->prob.K = std::min(k, k_cap);
+        unsigned long long st[VGB_STAT_COUNT];
+        if ((rc = run_pass(e, 0)) || (rc = vgb_engine_get_stats(e, st))) { free_engine(e); return rc; }
+        if (st[VGB_STAT_UNRESOLVED] == 0) {
+          float ms = 0.f;
+          cudaError_t te = cudaEventRecord(e->tev[0], e->st);
+          for (int r = 0; r < 2 && !rc && te == cudaSuccess; ++r) rc = run_pass(e, 0);
+          if (te == cudaSuccess) te = cudaEventRecord(e->tev[1], e->st);
+          if (te == cudaSuccess) te = cudaEventSynchronize(e->tev[1]);
+          if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e->tev[0], e->tev[1]);
+          if (!rc && te != cudaSuccess) {
+            set_error("K autotune timing: %s", cudaGetErrorString(te));
+            rc = VGB_ERR_CUDA;
+          }
+          if (rc) { free_engine(e); return rc; }
+          if (best < 0 || ms < best_ms) best = e->K, best_ms = ms;
+        }
+        if (e->K == k_cap) break;
+      }
+      e->K = e->prob.K = best > 0 ? best : std::min(MAX_SITE_K, k_cap);
+      e->timed = was;
+    } else {
+      // K: the smallest of 32, 48, 64, 96, 128 (at most n - 1) whose cells
+      // all reach the security radius -- more neighbours cannot change such
+      // a cell (the reference form has no completion pass)
+      for (int k : cand) {
+        e->K = e->prob.K = std::min(k, k_cap);
+        unsigned long long st[VGB_STAT_COUNT];
+        if ((rc = run_pass(e, 0)) || (rc = vgb_engine_get_stats(e, st))) { free_engine(e); return rc; }
+        if (st[VGB_STAT_SECURITY_MISS] == 0 || e->K == k_cap) break;
+      }
     }
-    if ((rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
   }
-  if (cfg.autotune && exact_form) {
-    if ((rc = tune_shapes(e)) || (rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
-  }
+  if (cfg.autotune && exact_form && (rc = tune_shapes(e))) { free_engine(e); return rc; }
+  if ((cfg.site_k == 0 || tune_exact) && (rc = vgb_engine_set_sites(e, sites))) { free_engine(e); return rc; }
   *out = e;
   return VGB_OK;
 }

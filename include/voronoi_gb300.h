@@ -111,8 +111,10 @@ enum vgb_buffer {
 
 typedef struct vgb_config {
   int site_k;   /* neighbours per site; the reference's compile-time _K_ (params.h:9);
-                   0 = autotune: the smallest of 32, 48, 64, 96, 128 whose cells all
-                   reach the security radius on the initial sites                    */
+                   0 = autotune on the initial sites: in the exact form the fastest
+                   of 32, 48, 64, 96, 128 whose pass leaves no cell unresolved (the
+                   completion pass makes cells exact whatever K); otherwise the
+                   smallest whose cells all reach the security radius             */
   int tet_k;    /* candidate sites per tet; 0 = the reference heuristic (voronoi.cu:936) */
   int grid_dim; /* site grid side; 0 = round((n/3.1)^(1/3)) (knearests.cu:243)           */
   int method;   /* VGB_METHOD_*                                                          */
@@ -131,20 +133,24 @@ typedef struct vgb_config {
                    which gives up on such a cell, with the exact fallback it lacks.
                    Makes degenerate inputs (sites on a regular lattice, cospherical
                    neighbours) come out whole.                                      */
-  int autotune; /* exact cell-tet form.  1: at creation, time the launch shapes on the
-                   initial sites and keep the fastest -- warps per kNN block (4 or 8),
-                   lanes per site in the first clip pass (8 or 16) and vertices per
-                   cell in the one-warp clip pass (64 or 96); results do not depend on
-                   them beyond float rounding.  0: the defaults (8, 8, 64).  The
-                   batched form tunes them with the grid density (grid_dim 0).       */
+  int autotune; /* exact cell-tet form.  1: at creation, time the launch shapes and
+                   keep the fastest -- warps per kNN block (4 or 8), lanes per site in
+                   the first clip pass (8 or 16), vertices per cell in the one-warp
+                   clip pass (64 or 96) -- and the clip form (tet_pieces); results do
+                   not depend on them beyond float rounding.  The choices are timed
+                   on the sites after two Lloyd steps (the initial sites are put
+                   back).  0: the defaults (8, 8, 64, the configured clip form).  The
+                   batched form tunes them with the grid density (grid_dim 0).      */
   int tet_pieces; /* cell-tet method.  0 (default): a copy of the cell is clipped by
                    each candidate tet's four faces, one warp per site.  1: each piece
                    (cell ^ tet) of a cell the first pass does not finish is built
                    from its tet, clipped by the cell faces that cross the tet, four
                    tets per warp (the pieces pass).  The same pieces up to float
-                   rounding; on relaxed uniform sites the first is about 10% faster
-                   (the pieces have a quarter of the cell's vertices, but each needs
-                   about eight cuts to the copy's four).                            */
+                   rounding.  The copies are faster when tets are about the cells'
+                   size (each piece is cut four times rather than about eight), the
+                   pieces when tets are much smaller than cells (a small tet cuts
+                   most of a copy away).  cfg.autotune times both and keeps the
+                   faster; the batched form always does.                            */
 } vgb_config;
 
 typedef struct vgb_engine vgb_engine;

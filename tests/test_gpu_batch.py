@@ -49,16 +49,15 @@ def test_batch_matches_lone_engines(pkg, meshgen, use_graph):
 
 
 def test_batch_volume_conserved(pkg, meshgen, oracle):
-    """With the autotuned K every cell reaches its security radius, so the
-    cells partition each mesh (at a fixed K=64 the FP64 oracle itself loses
-    conservation by 1e-5 on these cubes: corner cells miss it)."""
+    """With the autotuned K every cell is exact (its security radius reached,
+    or completed), so the cells partition each mesh (the FP64 oracle at a
+    fixed K=64 without completion loses conservation by 1e-5 on these
+    cubes: corner cells miss clipping neighbours)."""
     probs = _problems(meshgen)
     with pkg.Batch([(P.verts, P.tets, P.sites) for P in probs], site_k=0, tune_grid=False) as B:
         B.iterate(1, update=False)
         B.sync()
-        # the radius test is sufficient, not necessary: a few corner cells of
-        # the smallest cubes miss it even at the largest K and are still exact
-        assert B.stats()["security_miss"] <= 1e-3 * B.n_site
+        assert B.stats()["unresolved"] == 0
         for p, P in enumerate(probs):
             _, vol, _ = B.result(p)
             mv = oracle.mesh_volume(P.verts, P.tets)
@@ -67,9 +66,12 @@ def test_batch_volume_conserved(pkg, meshgen, oracle):
 
 
 def test_batch_autotune(pkg, meshgen):
-    """The chosen K is the smallest candidate whose cells all reach the
-    security radius (else the largest): a lone engine at that K reports no
-    security miss, one at the candidate below it does."""
+    """Per problem the chosen K is the smallest candidate whose cells all
+    reach the security radius (else the largest), or a smaller candidate
+    when the batch runs faster with every K capped there (the completion
+    pass keeps every cell exact): a lone engine at the chosen K leaves no
+    cell unresolved, and when it reports no security miss the candidate
+    below it does (the rule never overshoots)."""
     probs = _problems(meshgen)
     with pkg.Batch([(P.verts, P.tets, P.sites) for P in probs], site_k=0, tune_grid=True) as B:
         assert B.density in (1.5, pytest.approx(3.1), 6.0)
@@ -81,9 +83,9 @@ def test_batch_autotune(pkg, meshgen):
             with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, exact=True) as E:
                 E.iterate(1, update=False)
                 E.sync()
-                if K < 128:
-                    assert E.stats()["security_miss"] == 0
-                if K in (48, 64, 96, 128):
+                st = E.stats()
+                assert st["unresolved"] == 0
+                if st["security_miss"] == 0 and K in (48, 64, 96, 128):
                     smaller = {48: 32, 64: 48, 96: 64, 128: 96}[K]
                     with pkg.Engine(P.verts, P.tets, P.sites, site_k=smaller, exact=True) as E2:
                         E2.iterate(1, update=False)
@@ -101,19 +103,30 @@ def test_batch_invalid(pkg, meshgen):
         pkg.Batch([(P.verts, bad, P.sites)], site_k=16, tune_grid=False)
 
 
-def test_lone_engine_autotunes_k(pkg, meshgen):
-    """site_k=0 on a lone engine: the smallest candidate K with no security
-    miss (the batch rule), and the same K as a batch of that one problem."""
+def test_lone_engine_autotunes_k(pkg, meshgen, oracle):
+    """site_k=0 on a lone exact-form engine: the fastest candidate K whose
+    pass leaves no cell unresolved (the completion pass finishes every cell
+    its K nearest leave open, so K only moves work around); the cells at that
+    K are the oracle's exact cells and conserve the mesh volume."""
     P = meshgen.cube_problem(9, 3000, seed=2, jitter=0.1)
     with pkg.Engine(P.verts, P.tets, P.sites, site_k=0, exact=True) as E:
         K = E.site_k
         assert K in (32, 48, 64, 96, 128)
         E.iterate(1, update=False)
         E.sync()
-        if K < 128:
-            assert E.stats()["security_miss"] == 0
-    with pkg.Batch([(P.verts, P.tets, P.sites)], site_k=0, tune_grid=False) as B:
-        assert B.problem(0)["site_k"] == K
+        st = E.stats()
+        s4 = E.buffer("sites")
+        ids = s4[:, 3].copy().view(np.int32)
+        vol_g, mom_g = E.moments()
+    assert st["unresolved"] == 0 and st["tri_overflow"] == 0 and st["boundary_fail"] == 0
+    vol, mom = np.empty_like(vol_g), np.empty_like(mom_g)
+    vol[ids], mom[ids] = vol_g, mom_g
+    r = oracle.complete_cells(P.sites, np.arange(len(P.sites)), P.verts, P.tets, k0=128)
+    assert r["complete"].all()
+    big = r["vol"] > 1e-9 * r["vol"].max()
+    assert (np.abs(vol[big] - r["vol"][big]) / r["vol"][big]).max() < 1e-5
+    mv = oracle.mesh_volume(P.verts, P.tets)
+    assert abs(vol.sum() - mv) < 1e-6 * mv
 
 
 def test_autotuned_shapes_give_the_same_cells(pkg, meshgen, oracle):
