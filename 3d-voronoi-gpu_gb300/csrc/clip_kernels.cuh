@@ -75,12 +75,17 @@ namespace vgb {
 constexpr int CLIP_WARPS = 4;
 constexpr int BOX_PLANES = 6;
 // Resident blocks per SM the clip kernels are compiled for (the register
-// budget per thread is 65536 / (CLIP_WARPS * 32 * blocks)).
+// budget per thread is 65536 / (CLIP_WARPS * 32 * blocks)): measured, the
+// lone first pass is fastest at 8 (64 registers), the batched one at 7 (72,
+// where it spills nothing; 1% on the 256 Kuhn cubes).
 #ifndef VGB_CLIP_MIN_BLOCKS
 #define VGB_CLIP_MIN_BLOCKS 8
 #endif
 #ifndef VGB_BUILD_MIN_BLOCKS
 #define VGB_BUILD_MIN_BLOCKS 8
+#endif
+#ifndef VGB_BUILD_MIN_BLOCKS_BATCHED
+#define VGB_BUILD_MIN_BLOCKS_BATCHED 7
 #endif
 
 enum WarpCount : int {
@@ -993,8 +998,10 @@ constexpr int PIECE_TET0 = PIECE_FACES;  // the groups' tet faces: plane ids PIE
 // The queue is refilled a chunk of 32 candidates at a time while it holds
 // less than a round of pieces (one per group).
 constexpr int PIECE_QUEUE = WARP + PIECE_NG;
+// (7 resident blocks, 72 registers: 8% faster than 8 on the 256 Kuhn cubes,
+// 7% on the 1M-site torus)
 #ifndef VGB_PIECE_MIN_BLOCKS
-#define VGB_PIECE_MIN_BLOCKS 8
+#define VGB_PIECE_MIN_BLOCKS 7
 #endif
 
 struct PieceSmem {
@@ -1384,7 +1391,7 @@ __host__ __device__ constexpr int build_plane_stride(int kmax) { return 4 + kmax
 // counter independently; a warp's groups run one instruction stream, a
 // group whose cell is done passing its turn in each clip.
 template <bool BATCHED, int G, int SL, bool ROBUST>
-__global__ void __launch_bounds__(CLIP_WARPS * WARP, VGB_BUILD_MIN_BLOCKS) k_build(
+__global__ void __launch_bounds__(CLIP_WARPS * WARP, BATCHED ? VGB_BUILD_MIN_BLOCKS_BATCHED : VGB_BUILD_MIN_BLOCKS) k_build(
     const float4* __restrict__ sites, int n, const unsigned* __restrict__ knn, const ProbDesc* __restrict__ probs,
     const int* __restrict__ site_prob, const ProbDesc lone, dmom4* __restrict__ mom,
     unsigned long long* __restrict__ stats, const unsigned char* __restrict__ field,

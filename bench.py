@@ -4,7 +4,7 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--method cell_tet|site_major|plain]
                     [--reference-form] [--robust-predicates] [--accuracy M]
-                    [--no-cpu-baseline] [--no-forms]
+                    [--no-cpu-baseline] [--no-forms] [--no-autotune]
 
 A step is one Lloyd iteration of the path over the whole site set: grid sort,
 site kNN, per-tet reach, clipped cells (cell-tet method, exact form: cells
@@ -37,7 +37,9 @@ the batched form (256 problems); the small configuration (20^3 Kuhn cube,
 (cpu_baseline); and the SM clocks sampled during the timed region.  With
 --gpus N > 1 (torchrun), each rank runs an independent replica of the
 workload on its own GPU; value sums the replicas' iterations over the slowest
-rank's time.  --no-forms skips the extra forms and configurations.
+rank's time.  --no-forms skips the extra forms and configurations;
+--no-autotune keeps the default launch shapes (for profiling: every pass of
+the run is then a Lloyd step).
 
 --impl reference times the reference's own implementation of the path on the
 host cores instead (its kNN, centroid and clipping kernels compiled for the
@@ -338,7 +340,8 @@ def run_ours(args):
     K = w["K"]
     exact = args.method == "cell_tet" and not args.reference_form
     eng = pkg.Engine(P.verts, P.tets, P.sites, site_k=K, method=args.method, use_graph=True, device=local,
-                     exact=exact, robust_predicates=args.robust_predicates, autotune=exact)
+                     exact=exact, robust_predicates=args.robust_predicates,
+                     autotune=exact and not args.no_autotune)
     K = eng.site_k  # the autotuned K when the workload asks for one
     shape = eng.shape()  # the autotuned launch shapes (exact form)
 
@@ -865,6 +868,8 @@ def main():
                     help="decide near-zero vertex-vs-plane tests by exact determinant signs (off by default, "
                          "as the reference's arithmetic filter is)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="default launch shapes (profiling: every pass of the run is then a Lloyd step)")
     ap.add_argument("--accuracy", type=int, default=0, metavar="M",
                     help="also report per-iteration error against the FP64 oracle on M sampled sites")
     ap.add_argument("--accuracy-iters", type=int, default=20)
