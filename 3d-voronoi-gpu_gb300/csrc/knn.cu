@@ -18,7 +18,8 @@
 // Layout: one warp per query; consecutive warps take consecutive queries in
 // grid order, so the warps of a CTA read the same cells (L1 reuse).  The
 // warp visits the grid cells around the query's cell in Chebyshev shells
-// (the cell, then the 26 around it, ...), 32 cells at a time, one per lane;
+// (the cell with the 26 around it, then the next shell, ...), 32 cells at a
+// time, one per lane;
 // a cell whose box is farther than the current k-th distance is skipped.
 // The sites of the kept cells are then scanned 32 at a time, one per lane
 // (a warp scan of the cell counts maps lane -> site).  Each candidate is a
@@ -273,8 +274,15 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
     u64 tau = KEY_NONE;  // current k-th key
     int cnt = 0;         // buffered keys (warp-uniform)
     int filled = 0;      // keys merged into the list so far
-    for (int w = 0;; ++w) {
-      if (w > 0) {
+    // Shells 0 and 1 together (27 cells, table entries 0-26) when the query's
+    // own cell holds fewer than K sites: no stop test can fall between them,
+    // and one round of cells and candidates is saved.  A cell holding K or
+    // more (a dense cluster) goes first on its own, so its K-th key prunes
+    // the cells around it.
+    const int c0 = cbase + ci + dim * (cj + dim * ck);
+    const bool merge01 = cell_start[c0 + 1] - cell_start[c0] < K;
+    for (int w = merge01 ? 1 : 0;; ++w) {
+      if (w > (merge01 ? 1 : 0)) {
         if (ci - w < 0 && ci + w > dim - 1 && cj - w < 0 && cj + w > dim - 1 && ck - w < 0 && ck + w > dim - 1)
           break;  // no cell left
         if (tau != KEY_NONE) {
@@ -284,7 +292,8 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
           if (lb > 0.f && __uint_as_float((unsigned)(tau >> 32)) < lb * lb) break;
         }
       }
-      const int ncell = w == 0 ? 1 : (2 * w + 1) * (2 * w + 1) * (2 * w + 1) - (2 * w - 1) * (2 * w - 1) * (2 * w - 1);
+      const int ncell = w == 0 ? 1 : (w == 1 && merge01) ? 27
+                      : (2 * w + 1) * (2 * w + 1) * (2 * w + 1) - (2 * w - 1) * (2 * w - 1) * (2 * w - 1);
       for (int cb = 0; cb < ncell; cb += 32) {
         // one cell per lane: its site range, unless it is out of the grid
         // or farther than the current k-th distance
@@ -295,7 +304,7 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
           if (w > KNN_TAB_W) {
             shell_cell(w, t, di, dj, dk);
           } else if (w > 0) {
-            const unsigned u = shell_tab[(2 * w - 1) * (2 * w - 1) * (2 * w - 1) + t];
+            const unsigned u = shell_tab[((w == 1 && merge01) ? 0 : (2 * w - 1) * (2 * w - 1) * (2 * w - 1)) + t];
             di = (int)(u & 0xffu) - 8;
             dj = (int)((u >> 8) & 0xffu) - 8;
             dk = (int)(u >> 16) - 8;
