@@ -14,9 +14,9 @@ def _problems(meshgen):
     return [meshgen.cube_problem(n, ns, seed=s, jitter=0.1) for n, ns, s in SPECS]
 
 
-def _lone(pkg, P, K, n_iter):
+def _lone(pkg, P, K, n_iter, tet_pieces=False):
     """Sites, volumes and moments in input order from a lone engine."""
-    with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, exact=True) as E:
+    with pkg.Engine(P.verts, P.tets, P.sites, site_k=K, exact=True, tet_pieces=tet_pieces) as E:
         E.iterate(n_iter, update=True)
         E.sync()
         vol_g, mom_g = E.moments()
@@ -28,12 +28,14 @@ def _lone(pkg, P, K, n_iter):
         return E.sites_original(), vol, mom, E.grid_dim
 
 
-@pytest.mark.parametrize("use_graph", [True, False])
-def test_batch_matches_lone_engines(pkg, meshgen, use_graph):
+@pytest.mark.parametrize("use_graph,tet_pieces", [(True, False), (False, False), (True, True)])
+def test_batch_matches_lone_engines(pkg, meshgen, use_graph, tet_pieces):
+    """Each problem of the batch, in either clip form, bit for bit as a lone
+    engine with the same K, grid and form."""
     probs = _problems(meshgen)
     K = 32
     with pkg.Batch([(P.verts, P.tets, P.sites) for P in probs], site_k=K, tune_grid=False,
-                   use_graph=use_graph) as B:
+                   use_graph=use_graph, tet_pieces=tet_pieces) as B:
         assert B.n_prob == len(probs)
         assert B.n_site == sum(len(P.sites) for P in probs)
         B.iterate(2, update=True)
@@ -41,7 +43,7 @@ def test_batch_matches_lone_engines(pkg, meshgen, use_graph):
         for p, P in enumerate(probs):
             info = B.problem(p)
             xyz, vol, mom = B.result(p)
-            rx, rv, rm, rdim = _lone(pkg, P, K, 2)
+            rx, rv, rm, rdim = _lone(pkg, P, K, 2, tet_pieces)
             assert info["site_k"] == K and info["grid_dim"] == rdim
             assert np.array_equal(vol, rv), p
             assert np.array_equal(mom, rm), p
