@@ -991,7 +991,10 @@ __global__ void __launch_bounds__(CLIP_WARPS * WARP, SL >= 8 ? 2 : SL >= 4 ? 6 :
 // it, then the queue four pieces at a time; the pieces' moments go into the
 // site's compensated sums in queue order.  A piece that outgrows 32 vertices
 // sends the site to the 128-vertex pass (out_list), which redoes it with
-// copies of the cell.
+// copies of the cell.  This form pays when tets are much smaller than cells
+// (about 12 tets per site: 10% faster); at about 2 tets per site a piece
+// needs about eight cuts to a copy's four and the copies win by 8%
+// (vgb_config.tet_pieces; the autotuner times both).
 // ---------------------------------------------------------------------------
 constexpr int PIECE_G = 8, PIECE_SL = 4, PIECE_NG = WARP / PIECE_G;
 constexpr int PIECE_TET0 = PIECE_FACES;  // the groups' tet faces: plane ids PIECE_TET0 + 4 g + i
