@@ -107,6 +107,10 @@ def lib() -> C.CDLL:
     L.vgb_engine_set_graph.argtypes = [vp, i]
     L.vgb_engine_shape.argtypes = [vp, ip, ip, ip, ip]
     L.vgb_batch_shape.argtypes = [vp, ip, ip, ip, ip]
+    L.vgb_read_tet.argtypes = [C.c_char_p, C.POINTER(vp), ip, C.POINTER(vp), ip]
+    L.vgb_read_xyz.argtypes = [C.c_char_p, C.POINTER(vp), ip]
+    L.vgb_free_array.argtypes = [vp]
+    L.vgb_free_array.restype = None
     L.vgb_host_alloc.argtypes = [sz]
     L.vgb_host_alloc.restype = vp
     L.vgb_host_free.argtypes = [vp]
@@ -156,6 +160,44 @@ def device_describe(device: int = 0) -> str:
     buf = C.create_string_buffer(256)
     _check(lib().vgb_device_describe(device, buf, 256), "vgb_device_describe")
     return buf.value.decode()
+
+
+def _take_array(ptr: C.c_void_p, ctype, shape) -> np.ndarray:
+    """Copy a library-allocated array into numpy and release it."""
+    try:
+        n = int(np.prod(shape))
+        buf = (ctype * n).from_address(ptr.value) if n else (ctype * 0)()
+        return np.ctypeslib.as_array(buf).reshape(shape).copy()
+    finally:
+        lib().vgb_free_array(ptr)
+
+
+def load_tet(filename: str, normalize: bool = True):
+    """A `.tet` or `.vtk` tet mesh (test_voronoi.cu:40-119), numbers parsed on
+    every host thread by vgb_read_tet.  Returns float32 vertices (n, 3) and
+    int32 tets (m, 4), 0-based; with `normalize` the vertices are rescaled into
+    [0,1000]^3 by the reference's map (bounding box grown by 0.1% of its
+    longest side, then 1000 * (v - min) / longest side).  A file that cannot
+    be read raises VoronoiError (the reference returns false)."""
+    L = lib()
+    v, t = C.c_void_p(), C.c_void_p()
+    nv, nt = C.c_int(), C.c_int()
+    _check(L.vgb_read_tet(str(filename).encode(), C.byref(v), C.byref(nv), C.byref(t), C.byref(nt)),
+           "vgb_read_tet")
+    t_arr = _take_array(t, C.c_int, (nt.value, 4))
+    v_arr = _take_array(v, C.c_float, (nv.value, 3))
+    if normalize:
+        from .meshgen import normalize as _normalize
+        v_arr, _ = _normalize(v_arr)
+    return v_arr, t_arr
+
+
+def load_xyz_file(filename: str) -> np.ndarray:
+    """Sites of an `.xyz` file (test_voronoi.cu:134-145): float32 (n, 3), AoS,
+    parsed by vgb_read_xyz."""
+    xyz, n = C.c_void_p(), C.c_int()
+    _check(lib().vgb_read_xyz(str(filename).encode(), C.byref(xyz), C.byref(n)), "vgb_read_xyz")
+    return _take_array(xyz, C.c_float, (n.value, 3))
 
 
 def tet_k(n_site: int, n_tet: int, preferred: int = 0) -> int:

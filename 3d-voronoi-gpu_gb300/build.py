@@ -35,7 +35,7 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", f"-I{INC}", f"-I{CSRC}"]
 
 LIB_CU = ["grid.cu", "knn.cu", "clip.cu", "clip_robust.cu", "clip_plain.cu", "engine.cu", "kn_api.cu", "noalloc.cu",
           "batch.cu"]
-LIB_CPP = ["voronoi_api.cpp", "mesh_field.cpp", "kn_cxx.cpp"]
+LIB_CPP = ["voronoi_api.cpp", "mesh_field.cpp", "kn_cxx.cpp", "mesh_io.cpp"]
 
 
 def _nvcc() -> str:

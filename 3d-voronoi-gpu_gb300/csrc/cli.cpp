@@ -1,19 +1,19 @@
 // VolumeVoronoiGPU <tet_mesh.tet|vtk> <sites.xyz> <nb_iter> [k] [--site-k=N] [--robust-predicates]
 //
 // The reference's CLI (test_voronoi.cu:190-227): loads the mesh and
-// normalises it to [0,1000]^3 (test_voronoi.cu:14-121), loads the sites
-// (test_voronoi.cu:135-147; SoA when fewer than 14000 sites, as
+// normalises it to [0,1000]^3 (test_voronoi.cu:14-119), loads the sites
+// (test_voronoi.cu:134-145; SoA when fewer than 14000 sites, as
 // KNEARESTS_MIN_N in params.h:1 selects), runs nb_iter Lloyd iterations with
 // tet_k = k (0 or absent: the heuristic), and writes out.xyz, record.csv and
 // iter_<i>.xyz.  --site-k sets the neighbours per site (default 90);
 // --robust-predicates turns on the arithmetic filter with its exact fallback
 // (the reference's compile-time USE_ARITHMETIC_FILTER, params.h:27-32).
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
-#include <sstream>
 #include <string>
 #include <vector>
 
@@ -39,42 +39,17 @@ static void get_bbox(const std::vector<float>& v, float& xmin, float& ymin, floa
   xmax += d; ymax += d; zmax += d;
 }
 
+// The mesh (vgb_read_tet: parsed on every host thread), rescaled into
+// [0,1000]^3 like the reference's load_tet (test_voronoi.cu:102-117).
 static bool load_tet(const std::string& path, std::vector<float>& verts, std::vector<int>& idx) {
-  std::ifstream in(path);
-  if (in.fail()) return false;
-  std::string ext = path.substr(path.find_last_of('.') + 1), s;
-  int nv = 0, nt = 0, four = 0;
-  if (ext == "tet") {
-    in >> nv;
-    std::getline(in, s);
-    in >> nt;
-    std::getline(in, s);
-    verts.resize(3 * (size_t)nv);
-    idx.resize(4 * (size_t)nt);
-    for (size_t i = 0; i < 3 * (size_t)nv; ++i) in >> verts[i];
-    for (int t = 0; t < nt; ++t) {
-      in >> four >> idx[4 * (size_t)t] >> idx[4 * (size_t)t + 1] >> idx[4 * (size_t)t + 2] >> idx[4 * (size_t)t + 3];
-      if (four != 4) return false;
-    }
-  } else if (ext == "vtk") {
-    for (int i = 0; i < 4; ++i) std::getline(in, s);
-    in >> s >> nv >> s;
-    verts.resize(3 * (size_t)nv);
-    for (size_t i = 0; i < 3 * (size_t)nv; ++i) in >> verts[i];
-    in >> s >> nt >> s;
-    idx.resize(4 * (size_t)nt);
-    for (int t = 0; t < nt; ++t) {
-      in >> four;
-      if (four != 4) return false;
-      for (int j = 0; j < 4; ++j) {
-        in >> idx[4 * (size_t)t + j];
-        --idx[4 * (size_t)t + j];
-      }
-    }
-  } else {
-    return false;
-  }
-  if (in.fail() || nv <= 0 || nt <= 0) return false;
+  float* v = nullptr;
+  int* t = nullptr;
+  int nv = 0, nt = 0;
+  if (vgb_read_tet(path.c_str(), &v, &nv, &t, &nt) != VGB_OK) return false;
+  verts.assign(v, v + 3 * (size_t)nv);
+  idx.assign(t, t + 4 * (size_t)nt);
+  vgb_free_array(v);
+  vgb_free_array(t);
   float xmin, ymin, zmin, xmax, ymax, zmax;
   get_bbox(verts, xmin, ymin, zmin, xmax, ymax, zmax);
   float maxside = std::max(std::max(xmax - xmin, ymax - ymin), zmax - zmin);
@@ -89,17 +64,22 @@ static bool load_tet(const std::string& path, std::vector<float>& verts, std::ve
   return true;
 }
 
+// The sites (vgb_read_xyz), SoA when fewer than 14000 like the reference's
+// load_xyz_file (test_voronoi.cu:134-145).
 static bool load_xyz(const char* path, bool& soa, std::vector<float>& site, int& n) {
-  std::ifstream f(path);
-  if (f.fail() || !(f >> n) || n <= 1) return false;
+  float* s = nullptr;
+  if (vgb_read_xyz(path, &s, &n) != VGB_OK) return false;
+  if (n <= 1) {
+    vgb_free_array(s);
+    return false;
+  }
   soa = n < 14000;
   site.resize(3 * (size_t)n);
   for (int i = 0; i < n; ++i)
-    if (soa)
-      f >> site[i] >> site[i + (size_t)n] >> site[i + 2 * (size_t)n];
-    else
-      f >> site[3 * (size_t)i] >> site[3 * (size_t)i + 1] >> site[3 * (size_t)i + 2];
-  return !f.fail();
+    for (int d = 0; d < 3; ++d)
+      site[soa ? i + d * (size_t)n : 3 * (size_t)i + d] = s[3 * (size_t)i + d];
+  vgb_free_array(s);
+  return true;
 }
 
 static void drop_xyz(bool soa, const std::vector<float>& site, int n, const char* path) {
@@ -135,14 +115,14 @@ int main(int argc, char** argv) {
   std::vector<float> verts;
   std::vector<int> idx;
   if (!load_tet(pos[0], verts, idx)) {
-    std::cerr << pos[0] << ": could not load file" << std::endl;
+    std::cerr << pos[0] << ": could not load file (" << vgb_last_error() << ")" << std::endl;
     return 1;
   }
   bool soa = false;
   int n = 0;
   std::vector<float> site;
   if (!load_xyz(pos[1], soa, site, n)) {
-    std::cerr << pos[1] << ": could not load file" << std::endl;
+    std::cerr << pos[1] << ": could not load file (" << vgb_last_error() << ")" << std::endl;
     return 1;
   }
   int iters = std::atoi(pos[2]);

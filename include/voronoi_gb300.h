@@ -303,6 +303,24 @@ int vgb_batch_get_problem(vgb_batch* b, int p, float* xyz, double* vol, double* 
 /* Counters of the last pass over the whole batch: out[VGB_STAT_COUNT]. */
 int vgb_batch_get_stats(vgb_batch* b, unsigned long long* out);
 
+/* ---- Mesh and site files -------------------------------------------------
+ * The reference's file readers (test_voronoi.cu:40-145: load_tet and
+ * load_xyz_file), parsed on every host thread.  vgb_read_tet reads a .tet file
+ * ("<nv> vertices" line, "<nt> tets" line, nv "x y z", nt "4 a b c d",
+ * 0-based) or a .vtk file (four header lines, "POINTS nv type", coordinates,
+ * "CELLS nt size", nt "4 a b c d", 1-based, returned 0-based), chosen by the
+ * extension.  The coordinates are returned as written: the reference's CLI
+ * then rescales them into [0,1000]^3 (test_voronoi.cu:102-117), which the
+ * caller does.  vgb_read_xyz reads a count and then n "x y z" (AoS).  Each
+ * array is allocated by the call and released with vgb_free_array.  A
+ * missing file, an unknown extension, a bad header, too few numbers, a
+ * malformed number, a cell that is not "4 ..." or a vertex index out of range
+ * returns VGB_ERR_INVALID with the reason in vgb_last_error; nothing is
+ * allocated then. */
+int vgb_read_tet(const char* path, float** verts, int* n_vert, int** tets, int* n_tet);
+int vgb_read_xyz(const char* path, float** xyz, int* n);
+void vgb_free_array(void* p);
+
 #ifdef __cplusplus
 }
 #endif
