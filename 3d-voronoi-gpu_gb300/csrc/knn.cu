@@ -99,6 +99,11 @@ __device__ __forceinline__ void shell_cell(int w, int t, int& di, int& dj, int& 
   }
 }
 
+// Cells of Chebyshev shell w.
+__device__ __forceinline__ int shell_cells(int w) {
+  return w == 0 ? 1 : (2 * w + 1) * (2 * w + 1) * (2 * w + 1) - (2 * w - 1) * (2 * w - 1) * (2 * w - 1);
+}
+
 // Shells 0 .. KNN_TAB_W come from a table built once per block: entry
 // (2w-1)^3 + t holds the offset of the t-th cell of shell w, a byte per axis
 // biased by 8 (shell_cell costs a few integer divisions per cell).
@@ -223,9 +228,13 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
                                                         int k_tier, const int* __restrict__ q_list,
                                                         const int* __restrict__ q_count) {
   __shared__ u64 buf_all[W][KNN_BUF];
+  // each lane's site range(s) of the current round: start, n1, start2, and
+  // the sites of the lanes before it
+  __shared__ int rng_all[W][4][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
+  int(*rng)[32] = rng_all[wib];
   __shared__ unsigned shell_tab[KNN_TAB];
   shell_table(shell_tab);
   __syncthreads();
@@ -274,37 +283,51 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
     u64 tau = KEY_NONE;  // current k-th key
     int cnt = 0;         // buffered keys (warp-uniform)
     int filled = 0;      // keys merged into the list so far
-    // Shells 0 and 1 together (27 cells, table entries 0-26) when the query's
-    // own cell holds fewer than K sites: no stop test can fall between them,
-    // and one round of cells and candidates is saved.  A cell holding K or
-    // more (a dense cluster) goes first on its own, so its K-th key prunes
-    // the cells around it.
+    // The walk, one round of up to 32 site ranges (one per lane) at a time.
+    // Sites are sorted by cell, so the cells of an x-row are one contiguous
+    // range.  When the query's own cell holds fewer than K sites (no stop
+    // test can fall inside shells 0-1):
+    //   mode 1: shells 0 and 1 as the 9 x-rows of the 3x3x3 block;
+    //   mode 2: then, if the k-th distance so found cannot reach shell 3,
+    //           shell 2 as the x-rows of the 5x5 window, each cut to the
+    //           cells the k-th distance's ball meets (the two end cells
+    //           ci-2 and ci+2 for the rows through the block), and the walk
+    //           ends there.
+    // Otherwise (mode 0) shell w cell by cell, 32 cells a round, each cell
+    // farther than the k-th distance skipped, stopping once the k-th distance
+    // is below the distance to every cell beyond the shell.  A cell of K or
+    // more sites (a dense cluster) starts mode 0 at shell 0 on its own, so its
+    // K-th key prunes the cells around it.
     const int c0 = cbase + ci + dim * (cj + dim * ck);
     const bool merge01 = cell_start[c0 + 1] - cell_start[c0] < K;
-    for (int w = merge01 ? 1 : 0;; ++w) {
-      if (w > (merge01 ? 1 : 0)) {
-        if (ci - w < 0 && ci + w > dim - 1 && cj - w < 0 && cj + w > dim - 1 && ck - w < 0 && ck + w > dim - 1)
-          break;  // no cell left
-        if (tau != KEY_NONE) {
-          float lb = ring_bound(Q, ci, cj, ck, w, dim, h);
-          if (lb == FLT_MAX) break;
-          lb -= KNN_MARGIN;
-          if (lb > 0.f && __uint_as_float((unsigned)(tau >> 32)) < lb * lb) break;
+    int mode = merge01 ? 1 : 0, w = merge01 ? 1 : 0, cb = 0;
+    for (;;) {
+      // this lane's range(s): count sites from start, the first n1 of them
+      // (and the rest from start2 in mode 2's block rows)
+      int start = 0, count = 0, start2 = 0, n1 = 0;
+      if (mode == 0) {
+        // (after mode 1 this walk starts at w = 2, whose stop test mode 1's
+        // end repeats)
+        if (cb == 0 && w > 0) {
+          if (ci - w < 0 && ci + w > dim - 1 && cj - w < 0 && cj + w > dim - 1 && ck - w < 0 && ck + w > dim - 1)
+            break;  // no cell left
+          if (tau != KEY_NONE) {
+            float lb = ring_bound(Q, ci, cj, ck, w, dim, h);
+            if (lb == FLT_MAX) break;
+            lb -= KNN_MARGIN;
+            if (lb > 0.f && __uint_as_float((unsigned)(tau >> 32)) < lb * lb) break;
+          }
         }
-      }
-      const int ncell = w == 0 ? 1 : (w == 1 && merge01) ? 27
-                      : (2 * w + 1) * (2 * w + 1) * (2 * w + 1) - (2 * w - 1) * (2 * w - 1) * (2 * w - 1);
-      for (int cb = 0; cb < ncell; cb += 32) {
+        const int ncell = shell_cells(w);
         // one cell per lane: its site range, unless it is out of the grid
         // or farther than the current k-th distance
-        int start = 0, count = 0;
         const int t = cb + lane;
         if (t < ncell) {
           int di = 0, dj = 0, dk = 0;
           if (w > KNN_TAB_W) {
             shell_cell(w, t, di, dj, dk);
           } else if (w > 0) {
-            const unsigned u = shell_tab[((w == 1 && merge01) ? 0 : (2 * w - 1) * (2 * w - 1) * (2 * w - 1)) + t];
+            const unsigned u = shell_tab[(2 * w - 1) * (2 * w - 1) * (2 * w - 1) + t];
             di = (int)(u & 0xffu) - 8;
             dj = (int)((u >> 8) & 0xffu) - 8;
             dk = (int)(u >> 16) - 8;
@@ -317,50 +340,109 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
             count = cell_start[c + 1] - start;
           }
         }
-        int incl = count;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(KFULL, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const int total = __shfl_sync(KFULL, incl, 31);
-        for (int f0 = 0; f0 < total; f0 += 32) {
-          const int f = f0 + lane;
-          // the lane (cell) holding flat index f: first lane with incl > f
-          int lo = 0;
-#pragma unroll
-          for (int step = 16; step > 0; step >>= 1) {
-            const int v = __shfl_sync(KFULL, incl, lo + step - 1);
-            if (v <= f) lo += step;
-          }
-          const int cstart = __shfl_sync(KFULL, start, lo);
-          const int cexcl = __shfl_sync(KFULL, incl - count, lo);
-          u64 key = KEY_NONE;
-          if (f < total) {
-            const int p = cstart + (f - cexcl);
-            if (p != self) {
-              const float4 P = sites[p];
-              key = heap_key(dist2(Q, P), P);
+      } else {
+        // one x-row per lane: the 3x3 (mode 1) or 5x5 (mode 2) rows around the query's
+        const int r = mode == 1 ? 1 : 2, side = 2 * r + 1;
+        const int dj = lane % side - r, dk = lane / side - r;
+        const int j = cj + dj, k = ck + dk;
+        if (lane < side * side && j >= 0 && j < dim && k >= 0 && k < dim) {
+          const int row = cbase + dim * (j + dim * k);
+          if (mode == 1) {
+            start = cell_start[row + max(ci - 1, 0)];
+            count = cell_start[row + min(ci + 1, dim - 1) + 1] - start;
+          } else {
+            // the row's cells whose box (grown by the margin, as box_d2) lies
+            // within the k-th distance: the row's y-z distance leaves rho
+            // along x; 2 margins more cover the rounding of the bounds
+            float lo = (j == 0) ? -FLT_MAX : j * h - KNN_MARGIN;
+            float hi = (j == dim - 1) ? FLT_MAX : (j + 1) * h + KNN_MARGIN;
+            const float dy = fmaxf(fmaxf(lo - Q.y, Q.y - hi), 0.f);
+            lo = (k == 0) ? -FLT_MAX : k * h - KNN_MARGIN;
+            hi = (k == dim - 1) ? FLT_MAX : (k + 1) * h + KNN_MARGIN;
+            const float dz = fmaxf(fmaxf(lo - Q.z, Q.z - hi), 0.f);
+            const float rem = __uint_as_float((unsigned)(tau >> 32)) - (dy * dy + dz * dz);
+            if (rem >= 0.f) {
+              const float rho = sqrtf(rem) + 2.f * KNN_MARGIN;
+              const int fa = (int)fmaxf(fminf(floorf((Q.x - rho) / h), (float)dim), -1.f);
+              const int fb = (int)fmaxf(fminf(floorf((Q.x + rho) / h), (float)dim), -1.f);
+              const int a = max(max(ci - 2, 0), fa), b = min(min(ci + 2, dim - 1), fb);
+              if (dj >= -1 && dj <= 1 && dk >= -1 && dk <= 1) {
+                // mode 1 took ci-1 .. ci+1 of this row: its end cells only
+                if (a <= ci - 2 && ci - 2 <= b) {
+                  start = cell_start[row + ci - 2];
+                  n1 = cell_start[row + ci - 1] - start;
+                }
+                int n2 = 0;
+                if (a <= ci + 2 && ci + 2 <= b) {
+                  start2 = cell_start[row + ci + 2];
+                  n2 = cell_start[row + ci + 3] - start2;
+                }
+                count = n1 + n2;
+              } else if (a <= b) {
+                start = cell_start[row + a];
+                count = cell_start[row + b + 1] - start;
+                n1 = count;
+              }
             }
           }
-          const bool pass = key < tau;
-          const unsigned pm = __ballot_sync(KFULL, pass);
-          if (pass) buf[cnt + __popc(pm & lt_mask)] = key;
-          cnt += __popc(pm);
-          if (cnt >= 32) {
-            __syncwarp();
-            const u64 b = buf[lane];
-            const u64 rest = lane + 32 < cnt ? buf[lane + 32] : KEY_NONE;
-            __syncwarp();
-            if (lane + 32 < cnt) buf[lane] = rest;
-            cnt -= 32;
-            if (filled == 0) L[0] = warp_sort32(b, lane);  // nothing to merge with yet
-            else warp_merge<S>(L, b, lane);
-            filled += 32;
-            tau = kth_key<S>(L, K);
-            __syncwarp();
+        }
+      }
+      // the sites of the round, 32 at a time, one per lane (a warp scan of
+      // the counts maps lane -> site; the ranges wait in shared memory)
+      int incl = count;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(KFULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(KFULL, incl, 31);
+      rng[0][lane] = start;
+      rng[1][lane] = mode == 2 ? n1 : count;  // sites taken from start
+      rng[2][lane] = start2;
+      rng[3][lane] = incl - count;
+      __syncwarp();
+      for (int f0 = 0; f0 < total; f0 += 32) {
+        const int f = f0 + lane;
+        // the lane (range) holding flat index f: first lane with incl > f
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(KFULL, incl, lo + step - 1);
+          if (v <= f) lo += step;
+        }
+        u64 key = KEY_NONE;
+        if (f < total) {
+          const int o = f - rng[3][lo], n1o = rng[1][lo];
+          const int p = o < n1o ? rng[0][lo] + o : rng[2][lo] + (o - n1o);
+          if (p != self) {
+            const float4 P = sites[p];
+            key = heap_key(dist2(Q, P), P);
           }
         }
+        const bool pass = key < tau;
+        const unsigned pm = __ballot_sync(KFULL, pass);
+        if (pass) buf[cnt + __popc(pm & lt_mask)] = key;
+        cnt += __popc(pm);
+        if (cnt >= 32) {
+          __syncwarp();
+          const u64 b = buf[lane];
+          const u64 rest = lane + 32 < cnt ? buf[lane + 32] : KEY_NONE;
+          __syncwarp();
+          if (lane + 32 < cnt) buf[lane] = rest;
+          cnt -= 32;
+          if (filled == 0) L[0] = warp_sort32(b, lane);  // nothing to merge with yet
+          else warp_merge<S>(L, b, lane);
+          filled += 32;
+          tau = kth_key<S>(L, K);
+          __syncwarp();
+        }
+      }
+      __syncwarp();  // the ranges are read: the next round may write them
+      if (mode == 0) {
+        cb += 32;
+        if (cb < shell_cells(w)) continue;  // the shell's next 32 cells
+        cb = 0;
+        ++w;
       }
       // flush once the list can hold K keys (the stop test needs the k-th)
       if (cnt > 0 && filled + cnt >= K) {
@@ -371,19 +453,36 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
         tau = kth_key<S>(L, K);
         __syncwarp();
       }
+      if (mode == 2) break;  // shell 2 was the last the k-th distance reaches
+      if (mode == 1) {
+        // shells 0-1 done: stop, rows for shell 2, or cells from shell 2 on
+        w = 2;
+        mode = 0;
+        if (tau != KEY_NONE) {
+          const float td = __uint_as_float((unsigned)(tau >> 32));
+          float lb = ring_bound(Q, ci, cj, ck, 2, dim, h);
+          if (lb == FLT_MAX) break;
+          lb -= KNN_MARGIN;
+          if (lb > 0.f && td < lb * lb) break;
+          lb = ring_bound(Q, ci, cj, ck, 3, dim, h);
+          if (lb == FLT_MAX || (lb - KNN_MARGIN > 0.f && td < (lb - KNN_MARGIN) * (lb - KNN_MARGIN))) mode = 2;
+        }
+      }
     }
     if (cnt > 0) {
       __syncwarp();
       warp_absorb<S>(L, buf, cnt, filled, lane);
       __syncwarp();
     }
-    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * Kr : out + P.knn_off + (size_t)(qs - P.site_off) * Kr;
+    // the descriptor again (its row offsets were not kept through the walk)
+    const ProbDesc Po = CENTROIDS ? lone : prob_for(probs, site_prob, qs, lone, pq);
+    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * Kr : out + Po.knn_off + (size_t)(qs - Po.site_off) * Po.K;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int e = s * 32 + lane;
       if (e < K)
         orow_ptr[e] =
-            L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[P.site_off + (int)(L[s] & 0xffffffffu)];
+            L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[Po.site_off + (int)(L[s] & 0xffffffffu)];
     }
   }
 }
