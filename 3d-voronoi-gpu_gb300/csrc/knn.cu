@@ -110,7 +110,22 @@ __device__ __forceinline__ int shell_cells(int w) {
 constexpr int KNN_TAB_W = 4;
 constexpr int KNN_TAB = (2 * KNN_TAB_W + 1) * (2 * KNN_TAB_W + 1) * (2 * KNN_TAB_W + 1);
 
+// After them, KNN_BLOCK_LANES entries describe the lanes that take shells
+// 0-1 as x-rows: byte 0 dj, byte 1 dk, bytes 2-3 the first and last cell
+// along x relative to the query's (each biased by 8).  The query's own cell
+// comes first, then its two x-neighbours, the 4 rows beside its row and the
+// 4 diagonal rows, so that the first 32 keys -- which set the first k-th
+// distance -- are near ones even where hundreds of sites fill the block.
+constexpr int KNN_BLOCK_LANES = 11;
+// (dj, dk, first, last) of each lane, packed as above: (0,0,0,0), (0,0,-1,-1),
+// (0,0,1,1), (-1,0,-1,1), (1,0,-1,1), (0,-1,-1,1), (0,1,-1,1), (-1,-1,-1,1),
+// (1,-1,-1,1), (-1,1,-1,1), (1,1,-1,1)
+__constant__ unsigned KNN_BLOCK_LANE_TAB[KNN_BLOCK_LANES] = {
+    0x08080808u, 0x07070808u, 0x09090808u, 0x09070807u, 0x09070809u, 0x09070708u,
+    0x09070908u, 0x09070707u, 0x09070709u, 0x09070907u, 0x09070909u};
+
 __device__ __forceinline__ void shell_table(unsigned* tab) {
+  if (threadIdx.x < KNN_BLOCK_LANES) tab[KNN_TAB + threadIdx.x] = KNN_BLOCK_LANE_TAB[threadIdx.x];
   for (int i = threadIdx.x; i < KNN_TAB; i += blockDim.x) {
     int w = 0;
     while ((2 * w + 1) * (2 * w + 1) * (2 * w + 1) <= i) ++w;
@@ -235,7 +250,7 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
   const unsigned lt_mask = (1u << lane) - 1u;
   u64* buf = buf_all[wib];
   int(*rng)[32] = rng_all[wib];
-  __shared__ unsigned shell_tab[KNN_TAB];
+  __shared__ unsigned shell_tab[KNN_TAB + KNN_BLOCK_LANES];
   shell_table(shell_tab);
   __syncthreads();
   // with a work counter, warps draw the next query from it (one wave of
@@ -287,12 +302,14 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
     // Sites are sorted by cell, so the cells of an x-row are one contiguous
     // range.  When the query's own cell holds fewer than K sites (no stop
     // test can fall inside shells 0-1):
-    //   mode 1: shells 0 and 1 as the 9 x-rows of the 3x3x3 block;
+    //   mode 1: shells 0 and 1 as the 9 x-rows of the 3x3x3 block (the
+    //           query's row in three pieces, its own cell first);
     //   mode 2: then, if the k-th distance so found cannot reach shell 3,
     //           shell 2 as the x-rows of the 5x5 window, each cut to the
     //           cells the k-th distance's ball meets (the two end cells
     //           ci-2 and ci+2 for the rows through the block), and the walk
-    //           ends there.
+    //           ends there -- unless those rows hold more than 3K sites
+    //           (a cluster nearby): then mode 0 takes shell 2.
     // Otherwise (mode 0) shell w cell by cell, 32 cells a round, each cell
     // farther than the k-th distance skipped, stopping once the k-th distance
     // is below the distance to every cell beyond the shell.  A cell of K or
@@ -341,15 +358,21 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
           }
         }
       } else {
-        // one x-row per lane: the 3x3 (mode 1) or 5x5 (mode 2) rows around the query's
+        // one x-row (or part of one) per lane: mode 1 the 3x3 rows around the
+        // query's, as the table's lanes; mode 2 the 5x5 rows
         const int r = mode == 1 ? 1 : 2, side = 2 * r + 1;
-        const int dj = lane % side - r, dk = lane / side - r;
+        const unsigned u = shell_tab[KNN_TAB + (lane < KNN_BLOCK_LANES ? lane : 0)];
+        const int dj = mode == 1 ? (int)(u & 0xffu) - 8 : lane % side - r;
+        const int dk = mode == 1 ? (int)((u >> 8) & 0xffu) - 8 : lane / side - r;
         const int j = cj + dj, k = ck + dk;
-        if (lane < side * side && j >= 0 && j < dim && k >= 0 && k < dim) {
+        if (lane < (mode == 1 ? KNN_BLOCK_LANES : side * side) && j >= 0 && j < dim && k >= 0 && k < dim) {
           const int row = cbase + dim * (j + dim * k);
           if (mode == 1) {
-            start = cell_start[row + max(ci - 1, 0)];
-            count = cell_start[row + min(ci + 1, dim - 1) + 1] - start;
+            const int a = max(ci + (int)((u >> 16) & 0xffu) - 8, 0), b = min(ci + (int)(u >> 24) - 8, dim - 1);
+            if (a <= b) {
+              start = cell_start[row + a];
+              count = cell_start[row + b + 1] - start;
+            }
           } else {
             // the row's cells whose box (grown by the margin, as box_d2) lies
             // within the k-th distance: the row's y-z distance leaves rho
@@ -396,6 +419,12 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
         if (lane >= o) incl += y;
       }
       const int total = __shfl_sync(KFULL, incl, 31);
+      if (mode == 2 && total > 3 * K) {
+        // a dense part of shell 2 (near a cluster): its cells one by one,
+        // with the k-th distance tightening between rounds
+        mode = 0;
+        continue;
+      }
       rng[0][lane] = start;
       rng[1][lane] = mode == 2 ? n1 : count;  // sites taken from start
       rng[2][lane] = start2;
@@ -474,15 +503,24 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
       warp_absorb<S>(L, buf, cnt, filled, lane);
       __syncwarp();
     }
-    // the descriptor again (its row offsets were not kept through the walk)
-    const ProbDesc Po = CENTROIDS ? lone : prob_for(probs, site_prob, qs, lone, pq);
-    unsigned* orow_ptr = CENTROIDS ? out + (size_t)orow * Kr : out + Po.knn_off + (size_t)(qs - Po.site_off) * Po.K;
+    // the row offsets, read again (not kept through the walk)
+    long long row_off = (long long)orow * Kr;
+    int id_off = lone.site_off;
+    if (!CENTROIDS) {
+      if (probs) {
+        const ProbDesc* Pp = probs + site_prob[qs];
+        id_off = Pp->site_off;
+        row_off = Pp->knn_off + (long long)(qs - id_off) * Pp->K;
+      } else {
+        row_off = lone.knn_off + (long long)(qs - id_off) * lone.K;
+      }
+    }
+    unsigned* orow_ptr = out + row_off;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int e = s * 32 + lane;
       if (e < K)
-        orow_ptr[e] =
-            L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[Po.site_off + (int)(L[s] & 0xffffffffu)];
+        orow_ptr[e] = L[s] == KEY_NONE ? 0xffffffffu : (unsigned)pos_of_id[id_off + (int)(L[s] & 0xffffffffu)];
     }
   }
 }
