@@ -431,8 +431,8 @@ def run_ours(args):
                     "traffic": tr_knn[0] if tr_knn else None, "traffic_source": tr_knn[1] if tr_knn else None,
                     "peak_source": f"{peak_src} hbm_gbs", "bytes_per_launch": knn_bytes,
                     "ms_per_launch": round(phases["knn"], 4),
-                    "note": "the selection work per query (about 120 candidate keys, sorting networks) bounds "
-                            "this kernel, not its bytes; the 50%-of-HBM target is not met"}
+                    "note": "the walk and selection work per query (about 110 candidate keys, sorting "
+                            "networks) bounds this kernel, not its bytes; the 50%-of-HBM target is not met"}
 
     accuracy = None
     if rank == 0 and args.method == "cell_tet":
