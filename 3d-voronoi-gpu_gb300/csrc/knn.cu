@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
         continue;
       }
       rng[0][lane] = start;
-      rng[1][lane] = mode == 2 ? n1 : count;  // sites taken from start
+      rng[1][lane] = n1;  // mode 2: sites taken from start
       rng[2][lane] = start2;
       rng[3][lane] = incl - count;
       __syncwarp();
@@ -441,8 +441,12 @@ __global__ void __launch_bounds__(W * 32, 32 / W) k_knn(const float4* __restrict
         }
         u64 key = KEY_NONE;
         if (f < total) {
-          const int o = f - rng[3][lo], n1o = rng[1][lo];
-          const int p = o < n1o ? rng[0][lo] + o : rng[2][lo] + (o - n1o);
+          const int o = f - rng[3][lo];
+          int p = rng[0][lo] + o;
+          if (mode == 2) {  // only mode 2's block rows have a second range
+            const int n1o = rng[1][lo];
+            if (o >= n1o) p = rng[2][lo] + (o - n1o);
+          }
           if (p != self) {
             const float4 P = sites[p];
             key = heap_key(dist2(Q, P), P);
