@@ -18,11 +18,12 @@
 // Layout: one warp per query; consecutive warps take consecutive queries in
 // grid order, so the warps of a CTA read the same cells (L1 reuse).  The
 // warp visits the grid cells around the query's cell in Chebyshev shells
-// (the cell with the 26 around it, then the next shell, ...), 32 cells at a
-// time, one per lane;
-// a cell whose box is farther than the current k-th distance is skipped.
-// The sites of the kept cells are then scanned 32 at a time, one per lane
-// (a warp scan of the cell counts maps lane -> site).  Each candidate is a
+// (the cell with the 26 around it, then the next shell, ...), up to 32 site
+// ranges a round, one per lane: where it can, a range is an x-row of cells
+// (sites are sorted by cell, so a row's sites are contiguous), otherwise one
+// cell; cells farther than the current k-th distance are left out.  The
+// sites of a round are then scanned 32 at a time, one per lane (a warp scan
+// of the range lengths maps lane -> site).  Each candidate is a
 // 64-bit key (distance bits << 32 | id).  Keys below the current k-th key go
 // to a per-warp buffer in shared memory; 32 buffered keys are sorted with a
 // bitonic network across the lanes and merged into the warp's sorted list of
