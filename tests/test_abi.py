@@ -68,6 +68,38 @@ def test_cpp_drop_in_header_compiles(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_c_abi_from_c99(built, tmp_path):
+    """A plain C99 caller includes the C ABI header, links the library and
+    calls the file readers (host code: no GPU needed), error path included."""
+    src = tmp_path / "use.c"
+    src.write_text(r'''#include <stdio.h>
+#include "voronoi_gb300.h"
+int main(int argc, char** argv) {
+  float* v = 0; int* t = 0; int nv = 0, nt = 0, n = 0; float* s = 0;
+  if (argc < 3) return 1;
+  if (vgb_read_tet(argv[1], &v, &nv, &t, &nt) != VGB_OK) { fprintf(stderr, "%s\n", vgb_last_error()); return 2; }
+  if (vgb_read_xyz(argv[2], &s, &n) != VGB_OK) { fprintf(stderr, "%s\n", vgb_last_error()); return 3; }
+  printf("%d %d %d %.9g %d %.9g\n", nv, nt, n, v[3 * nv - 1], t[4 * nt - 1], s[3 * n - 1]);
+  vgb_free_array(v); vgb_free_array(t); vgb_free_array(s);
+  if (vgb_read_tet("missing.tet", &v, &nv, &t, &nt) != VGB_ERR_INVALID) return 4;
+  printf("%s\n", vgb_last_error());
+  return 0;
+}
+''')
+    (tmp_path / "m.tet").write_text("4 vertices\n1 tets\n0 0 0\n1 0 0\n0 1 0\n0 0 1.5\n4 0 1 2 3\n")
+    (tmp_path / "s.xyz").write_text("2\n1 2 3\n4 5 6.25\n")
+    lib_dir = Path(built).parent
+    exe = tmp_path / "use"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-pedantic", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                        f"-L{lib_dir}", "-lvoronoi_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), str(tmp_path / "m.tet"), str(tmp_path / "s.xyz")], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split("\n")[:2] == ["4 1 2 1.5 3 6.25", "missing.tet: cannot read"]
+
+
 def test_cli_built(built, pkg):
     assert Path(pkg.CLI_PATH).exists()
 
