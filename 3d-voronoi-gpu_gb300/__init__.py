@@ -14,6 +14,10 @@ Mirrors of the reference's entry points:
                                   include/voronoi_gb300.h (one object per
                                   mesh + site set; Lloyd iterations stay on
                                   the GPU).
+  * Batch                      -- many independent problems per launch.
+  * load_tet / load_xyz_file   -- the mesh and site file loaders
+                                  (test_voronoi.cu:40-145), parsed on every
+                                  host thread by vgb_read_tet / vgb_read_xyz.
 """
 from __future__ import annotations
 
