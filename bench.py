@@ -324,15 +324,49 @@ def dist_env():
     return world, rank, local
 
 
-def run_ours(args):
-    world, rank, local = dist_env()
-    dist = None
-    if world > 1:
+class Replicas:
+    """The N independent replicas of a bench run (one process per GPU, as
+    torchrun starts them; the path has no exchange step, so there is no
+    collective on the data path).  Gives each process its rank and GPU and
+    the two things the timed region needs across ranks: a barrier on both
+    sides, and the slowest rank's time.  One process needs no process group;
+    several use NCCL on GPUs, gloo where there are none."""
+
+    def __init__(self):
+        self.world, self.rank, self.local = dist_env()
+        self.dist = None
+        self.device = "cpu"
+        if self.world > 1:
+            import torch
+            import torch.distributed as tdist
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+                self.device = f"cuda:{self.local}"
+            tdist.init_process_group("nccl" if self.device != "cpu" else "gloo")
+            self.dist = tdist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        """x on the slowest rank (the timed region's duration over all replicas)."""
+        if not self.dist:
+            return x
         import torch
-        import torch.distributed as tdist
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        dist = tdist
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def run_ours(args):
+    R = Replicas()
+    world, rank, local = R.world, R.rank, R.local
     pkg = load_package()
     pkg.build()
     w = WORKLOADS[args.workload]
@@ -345,17 +379,7 @@ def run_ours(args):
     K = eng.site_k  # the autotuned K when the workload asks for one
     shape = eng.shape()  # the autotuned launch shapes (exact form)
 
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = R.barrier, R.max
 
     # warm-up (graph capture happens on the first replay)
     eng.time_iterate(args.warmup, update=True)
@@ -668,14 +692,8 @@ def batch_measure(pkg, warmup, steps, device):
 def run_batch(args):
     """The batched form: every problem of the batch advances one Lloyd
     iteration per step, one launch per kernel for the whole batch."""
-    world, rank, local = dist_env()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as tdist
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        dist = tdist
+    R = Replicas()
+    world, rank, local = R.world, R.rank, R.local
     pkg = load_package()
     pkg.build()
     import voronoi_gb300.meshgen as mg
@@ -686,17 +704,14 @@ def run_batch(args):
                   device=local)
     create_s = time.perf_counter() - t0
     B.time_iterate(args.warmup, update=True)
-    if dist:
-        dist.barrier()
+    R.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     ms = B.time_iterate(args.steps, update=True)
     clk = clocks.stop()
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    B.sync()
+    R.barrier()
+    ms = R.max(ms)
     value = world * args.steps / (ms / 1e3)
     stats = B.stats()
     ks = collections.Counter(B.problem(p)["site_k"] for p in range(B.n_prob))
